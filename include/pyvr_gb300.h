@@ -1,0 +1,114 @@
+/*
+ * pyvr_gb300 -- C ABI of the GB300 (sm_103a) volume ray marcher.
+ *
+ * Replaces the GL path behind pyvr's VolumeRenderer
+ * (pyvr/moderngl_renderer/renderer.py + manager.py + pyvr/shaders/volume.*.glsl).
+ * Plain C types only: host pointers, device pointers as void*, sizes as ints,
+ * a CUDA stream as void* (NULL = the renderer's own stream).
+ *
+ * Every function returns PVR_OK (0) or an error code; pvr_last_error()
+ * gives the message of the calling thread's most recent error.  The Python
+ * shim maps PVR_ERR_VALUE -> ValueError, PVR_ERR_TYPE -> TypeError,
+ * PVR_ERR_STATE / PVR_ERR_CUDA -> RuntimeError, PVR_ERR_NOMEM -> MemoryError,
+ * following the reference's conventions (renderer.py:77-87, 122-127;
+ * manager.py:87-88, 120-121, 190-225).
+ *
+ * Threading: a handle is driven by one thread at a time (like the single GL
+ * context of manager.py:26); different handles may be used concurrently.
+ */
+#ifndef PYVR_GB300_H
+#define PYVR_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PVR_ABI_VERSION 1
+
+enum pvr_status {
+    PVR_OK = 0,
+    PVR_ERR_VALUE = 1,       /* bad argument value (ValueError)            */
+    PVR_ERR_TYPE = 2,        /* unsupported dtype / kind (TypeError)       */
+    PVR_ERR_STATE = 3,       /* call order / missing state (RuntimeError)  */
+    PVR_ERR_CUDA = 4,        /* CUDA runtime error (RuntimeError)          */
+    PVR_ERR_NOMEM = 5,       /* device allocation failed (MemoryError)     */
+    PVR_ERR_TIMEOUT = 6      /* bounded wait expired (TimeoutError)        */
+};
+
+enum pvr_dtype { PVR_U8 = 0, PVR_F16 = 1, PVR_F32 = 2 };
+
+typedef struct pvr_renderer pvr_renderer;
+
+/* Library identity. */
+int pvr_abi_version(void);
+const char *pvr_last_error(void);
+
+/* ModernGLManager(width, height) + shader load (manager.py:14-41, 43-75;
+ * renderer.py:34-105).  Binds to the current CUDA device; creates the
+ * handle's stream and its RGBA8 target.  Default state matches the
+ * reference constructor: bounds +-0.5 (renderer.py:101-102), balanced config
+ * (renderer.py:70-73), Light.default() (renderer.py:82-83). */
+int pvr_create(int width, int height, pvr_renderer **out);
+
+/* ModernGLManager.cleanup (manager.py:238-256): frees every device buffer. */
+int pvr_destroy(pvr_renderer *r);
+
+/* load_volume voxel part: create_volume_texture + bounds uniforms
+ * (renderer.py:107-141, manager.py:77-108).  `data` is the host (D,H,W)
+ * C-order array in its own storage type; it stays in that type on the device.
+ * `value_scale` multiplies the interpolated stored value (1.0 reproduces the
+ * reference, which samples uint8 voxels as 0..255; 1/255 reads them as
+ * UNORM).  Clears any normals of the previous volume. */
+int pvr_load_volume(pvr_renderer *r, const void *data, int dtype, int d, int h, int w,
+                    float value_scale, const float min_bounds[3], const float max_bounds[3]);
+
+/* load_volume normal part: create_normal_texture (manager.py:110-135).
+ * `normals` is host float32 (D,H,W,3) for the loaded volume, or NULL to drop
+ * them (the march then shades with normalize(density, 0, 0), which is what
+ * the reference's unbound normal sampler reads, renderer.py:143-146). */
+int pvr_load_normals(pvr_renderer *r, const float *normals);
+
+/* set_transfer_functions -> create_rgba_transfer_function_texture
+ * (renderer.py:190-207, manager.py:137-186): `rgba` is host float32
+ * (size, 4).  Replaces the previous table (the reference leaks one). */
+int pvr_set_lut(pvr_renderer *r, const float *rgba, int size);
+
+/* set_camera (renderer.py:148-172): the raw float32 bytes of
+ * Camera.get_view_matrix() and get_projection_matrix(w/h) as numpy holds
+ * them (read column-major, as GL does, manager.py:188-192) and the camera
+ * position.  Both inverses are formed here in double. */
+int pvr_set_camera(pvr_renderer *r, const float view[16], const float proj[16],
+                   const float camera_pos[3]);
+
+/* set_light -> _update_light (renderer.py:174-188, 311-316). */
+int pvr_set_light(pvr_renderer *r, const float position[3], const float target[3],
+                  float ambient, float diffuse);
+
+/* set_config -> _update_render_config (renderer.py:229-249, 303-309). */
+int pvr_set_config(pvr_renderer *r, float step_size, int max_steps, float reference_step_size);
+
+/* render() (renderer.py:209-219): clear, march, blend, read back.
+ * out_rgba8: host buffer of width*height*4 bytes, bottom row first
+ * (manager.py:228-230).  out_rgba32f: optional host buffer of
+ * width*height*4 floats receiving the pre-blend fragment colour.
+ * Synchronous.  With no volume loaded the image is transparent black. */
+int pvr_render(pvr_renderer *r, uint8_t *out_rgba8, float *out_rgba32f);
+
+/* Same march into caller-owned DEVICE buffers on `stream` (NULL = the
+ * handle's stream); asynchronous, no host copy.  Either output may be NULL. */
+int pvr_render_device(pvr_renderer *r, void *d_rgba8, void *d_rgba32f, void *stream);
+
+/* In-box samples (loop iterations whose texture coordinate is valid,
+ * volume.frag.glsl:92) counted by the most recent render on this handle;
+ * waits for that render. */
+int pvr_last_sample_count(pvr_renderer *r, long long *samples);
+
+/* Bytes of device memory this handle holds. */
+int pvr_device_bytes(pvr_renderer *r, long long *bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PYVR_GB300_H */

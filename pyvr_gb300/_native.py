@@ -1,0 +1,146 @@
+"""Build and load ``libpyvr_gb300.so``, the CUDA (sm_103a) library behind the C ABI
+declared in ``include/pyvr_gb300.h``.
+
+The library is compiled in-tree with nvcc (one object per ``csrc/*.cu``, built
+in parallel, then linked).  There is no CPU fallback: if the library cannot
+be built or loaded, every renderer call raises.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import shutil
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+INCLUDE = os.path.join(ROOT, "include")
+BUILD = os.path.join(PKG, "_build")
+LIB_PATH = os.path.join(PKG, "libpyvr_gb300.so")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# --fmad=false: no implicit multiply-add contraction; the kernels write
+# fmaf() where a fused operation is meant (see csrc/pvr_device.cuh).
+NVCC_FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
+              "-Xcompiler", "-fno-fast-math", f"-I{INCLUDE}"]
+
+# status codes of include/pyvr_gb300.h
+PVR_OK, PVR_ERR_VALUE, PVR_ERR_TYPE, PVR_ERR_STATE, PVR_ERR_CUDA, PVR_ERR_NOMEM, PVR_ERR_TIMEOUT = range(7)
+PVR_U8, PVR_F16, PVR_F32 = 0, 1, 2
+
+
+def nvcc() -> str:
+    exe = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(exe):
+        raise RuntimeError("nvcc not found: the pyvr_gb300 CUDA library cannot be built")
+    return exe
+
+
+def _sources():
+    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
+
+
+def _deps():
+    files = _sources() + [os.path.join(CSRC, f) for f in os.listdir(CSRC)
+                          if f.endswith((".cuh", ".h"))]
+    files.append(os.path.join(INCLUDE, "pyvr_gb300.h"))
+    return files
+
+
+def needs_build() -> bool:
+    if not os.path.exists(LIB_PATH):
+        return True
+    t = os.path.getmtime(LIB_PATH)
+    return any(os.path.getmtime(f) > t for f in _deps())
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    """Compile every csrc/*.cu for sm_103a and link the shared library."""
+    if not force and not needs_build():
+        return LIB_PATH
+    os.makedirs(BUILD, exist_ok=True)
+    exe = nvcc()
+
+    def compile_one(src):
+        obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
+        cmd = [exe, *ARCH, *NVCC_FLAGS, "-c", src, "-o", obj]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed on {src}:\n{r.stderr}")
+        if verbose and r.stderr:
+            print(r.stderr)
+        return obj
+
+    with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 1)) as ex:
+        objs = list(ex.map(compile_one, _sources()))
+    tmp = LIB_PATH + f".tmp{os.getpid()}"
+    cmd = [exe, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart_static", "-lrt", "-lpthread", "-ldl"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc link failed:\n{r.stderr}")
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+_lib = None
+
+# exported symbol -> (restype, argtypes)
+_VP, _I, _F, _LL = ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_longlong
+_FP = ctypes.POINTER(ctypes.c_float)
+SIGNATURES = {
+    "pvr_abi_version": (_I, []),
+    "pvr_last_error": (ctypes.c_char_p, []),
+    "pvr_create": (_I, [_I, _I, ctypes.POINTER(_VP)]),
+    "pvr_destroy": (_I, [_VP]),
+    "pvr_load_volume": (_I, [_VP, _VP, _I, _I, _I, _I, _F, _FP, _FP]),
+    "pvr_load_normals": (_I, [_VP, _VP]),
+    "pvr_set_lut": (_I, [_VP, _VP, _I]),
+    "pvr_set_camera": (_I, [_VP, _FP, _FP, _FP]),
+    "pvr_set_light": (_I, [_VP, _FP, _FP, _F, _F]),
+    "pvr_set_config": (_I, [_VP, _F, _I, _F]),
+    "pvr_render": (_I, [_VP, _VP, _VP]),
+    "pvr_render_device": (_I, [_VP, _VP, _VP, _VP]),
+    "pvr_last_sample_count": (_I, [_VP, ctypes.POINTER(_LL)]),
+    "pvr_device_bytes": (_I, [_VP, ctypes.POINTER(_LL)]),
+}
+
+
+def load(path: str = LIB_PATH, build_if_missing: bool = True):
+    """Load (building first if needed) and type the exported functions."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build_if_missing and (not os.path.exists(path) or (path == LIB_PATH and needs_build())):
+        build()
+    if not os.path.exists(path):
+        raise RuntimeError(f"pyvr_gb300 CUDA library missing at {path}")
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+class PvrError(RuntimeError):
+    pass
+
+
+_EXC = {PVR_ERR_VALUE: ValueError, PVR_ERR_TYPE: TypeError, PVR_ERR_STATE: RuntimeError,
+        PVR_ERR_CUDA: RuntimeError, PVR_ERR_NOMEM: MemoryError, PVR_ERR_TIMEOUT: TimeoutError}
+
+
+def check(rc: int) -> None:
+    """Raise the Python exception the reference would raise for this status."""
+    if rc == PVR_OK:
+        return
+    msg = _lib.pvr_last_error().decode(errors="replace") if _lib is not None else f"status {rc}"
+    raise _EXC.get(rc, PvrError)(msg)
+
+
+def fptr(arr):
+    return arr.ctypes.data_as(_FP)

@@ -1,0 +1,144 @@
+"""Seeded synthetic scenes for the benchmark and test configurations.
+
+No dataset is involved anywhere: every volume, camera and transfer function
+is generated here from a seed.  Colour maps that the configurations name by
+matplotlib names ("viridis", "the 12 built-ins") are replaced by clearly
+labelled stand-ins -- seeded piecewise-linear RGB ramps -- because
+matplotlib's tables are not available; the LUT is an input to both the
+renderer and the oracle, so parity does not depend on it.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+from .camera import Camera
+from .config import RenderConfig
+from .lighting import Light
+from .transferfunctions import ColorTransferFunction, OpacityTransferFunction
+from .volume import Volume, compute_normal_volume
+
+N_STANDIN_COLORMAPS = 12
+
+
+def double_sphere(n: int = 64) -> np.ndarray:
+    """max over centres (+-0.4, 0, 0) of clip(1 - |p - c| / 0.5, 0, 1) on the
+    grid linspace(-1, 1, n)^3, indexing 'ij' (array axis 0 = world x)."""
+    g = np.linspace(-1.0, 1.0, n)
+    x, y, z = np.meshgrid(g, g, g, indexing="ij")
+    out = np.zeros((n, n, n))
+    for cx in (0.4, -0.4):
+        r = np.sqrt((x - cx) ** 2 + y ** 2 + z ** 2)
+        out = np.maximum(out, np.clip(1.0 - r / 0.5, 0.0, 1.0))
+    return out.astype(np.float32)
+
+
+def _upsample_axis(a: np.ndarray, axis: int, n: int) -> np.ndarray:
+    """Linear interpolation along one axis, align-corners (end samples kept)."""
+    m = a.shape[axis]
+    x = np.linspace(0.0, m - 1.0, n)
+    i0 = np.minimum(np.floor(x).astype(np.int64), m - 2) if m > 1 else np.zeros(n, np.int64)
+    w = (x - i0) if m > 1 else np.zeros(n)
+    a0 = np.take(a, i0, axis=axis)
+    a1 = np.take(a, np.minimum(i0 + 1, m - 1), axis=axis)
+    shape = [1] * a.ndim
+    shape[axis] = n
+    w = w.reshape(shape).astype(a.dtype)
+    return a0 + w * (a1 - a0)
+
+
+def value_noise(shape, seed: int, lattices=(8, 16, 32, 64)) -> np.ndarray:
+    """4-octave value noise in [0, 1]: uniform[0,1] lattices of 8^3 .. 64^3
+    from ``default_rng(seed)``, each trilinearly upsampled to ``shape``
+    (align-corners), weighted 0.5^k, summed and min-max normalised."""
+    rng = np.random.default_rng(seed)
+    acc = np.zeros(shape, dtype=np.float32)
+    for k, lat in enumerate(lattices):
+        v = rng.random((lat, lat, lat), dtype=np.float32)
+        for axis in range(3):
+            v = _upsample_axis(v, axis, shape[axis])
+        acc += np.float32(0.5 ** k) * v
+    lo, hi = acc.min(), acc.max()
+    return ((acc - lo) / (hi - lo)).astype(np.float32)
+
+
+def standin_colormap(index: int, lut_size: int = 256) -> ColorTransferFunction:
+    """Stand-in for a named matplotlib colour map: 6 seeded RGB control points."""
+    rng = np.random.default_rng(7000 + int(index))
+    xs = np.linspace(0.0, 1.0, 6)
+    cs = rng.random((6, 3))
+    return ColorTransferFunction([(float(x), tuple(map(float, c))) for x, c in zip(xs, cs)],
+                                 lut_size=lut_size)
+
+
+def random_opacity(rng: np.random.Generator, n_points: int, hi: float,
+                   lut_size: int = 256) -> OpacityTransferFunction:
+    xs = np.sort(rng.random(n_points))
+    ys = rng.uniform(0.0, hi, n_points)
+    return OpacityTransferFunction([(float(x), float(y)) for x, y in zip(xs, ys)],
+                                   lut_size=lut_size)
+
+
+def to_storage(v: np.ndarray, dtype: str) -> np.ndarray:
+    """[0,1] float volume -> uint8 (round(v*255)), float16 or float32."""
+    if dtype == "u8":
+        return np.rint(v * 255.0).astype(np.uint8)
+    if dtype == "f16":
+        return v.astype(np.float16)
+    return v.astype(np.float32)
+
+
+# ---------------------------------------------------------------------------
+# Configurations
+# ---------------------------------------------------------------------------
+
+def config_small():
+    """64^3 float32 double sphere on [-1,1]^3, 256x256, balanced."""
+    data = double_sphere(64)
+    vol = Volume(data=data, normals=compute_normal_volume(data),
+                 min_bounds=np.array([-1.0, -1.0, -1.0], np.float32),
+                 max_bounds=np.array([1.0, 1.0, 1.0], np.float32))
+    cam = Camera.from_spherical(target=np.zeros(3, np.float32), azimuth=np.pi / 4,
+                                elevation=np.pi / 6, roll=0.0, distance=3.0, fov=np.pi / 4)
+    light = Light.directional([1, -1, 0], ambient=0.2, diffuse=0.8)
+    ctf = standin_colormap(0)
+    otf = OpacityTransferFunction.linear(0.0, 0.1)
+    return dict(volume=vol, camera=cam, light=light, ctf=ctf, otf=otf,
+                config=RenderConfig.balanced(), width=256, height=256, value_scale=1.0)
+
+
+def config_scale_volume(n: int = 256, seed: int = 0) -> np.ndarray:
+    return value_noise((n, n, n), seed)
+
+
+def config_scale(dtype: str = "f32", n: int = 256, res: int = 1024, noise=None):
+    """256^3 value noise (seed 0) in u8/f16/f32, 16 orbit cameras, 1024^2,
+    high_quality, 8 seeded opacity points in [0, 0.3] + stand-in colour."""
+    v = config_scale_volume(n) if noise is None else noise
+    data = to_storage(v, dtype)
+    # normals by central differences of the stored values, as pyvr computes them
+    normals = compute_normal_volume(data)
+    vol = Volume(data=data, normals=normals,
+                 min_bounds=np.array([-1.0, -1.0, -1.0], np.float32),
+                 max_bounds=np.array([1.0, 1.0, 1.0], np.float32))
+    cams = [Camera.from_spherical(target=np.zeros(3, np.float32), azimuth=2 * np.pi * k / 16,
+                                  elevation=np.pi / 6, roll=0.0, distance=3.0)
+            for k in range(16)]
+    otf = random_opacity(np.random.default_rng(0), 8, 0.3)
+    return dict(volume=vol, cameras=cams, light=Light.directional([1, -1, 0], 0.2, 0.8),
+                ctf=standin_colormap(0), otf=otf, config=RenderConfig.high_quality(),
+                width=res, height=res, value_scale=(1.0 / 255.0 if dtype == "u8" else 1.0))
+
+
+def frame_inputs(volume: Volume, camera, light, config, lut: np.ndarray, width: int,
+                 height: int, value_scale: float = 1.0) -> dict:
+    """Everything one frame depends on, as the uniforms/textures the reference
+    renderer would set (renderer.py:107-172, 303-316), in a plain dict."""
+    from .renderer import camera_uniforms
+    view, proj, pos = camera_uniforms(camera, width, height)
+    return dict(width=width, height=height, view=view, proj=proj, cam_pos=pos,
+                volume=volume.data, normals=volume.normals, value_scale=value_scale,
+                bmin=volume.min_bounds, bmax=volume.max_bounds, lut=lut,
+                step_size=config.step_size, reference_step_size=config.reference_step_size,
+                max_steps=config.max_steps, light_pos=light.position, light_target=light.target,
+                ambient=light.ambient_intensity, diffuse=light.diffuse_intensity)

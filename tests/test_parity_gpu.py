@@ -1,0 +1,204 @@
+"""GPU parity: the CUDA march through the C ABI against the CPU oracle.
+
+Bar (stated per north-star): RGBA8 within 1 LSB per channel on >= 99.9% of
+pixels and never more than 2 LSB; the float image within 1e-6 absolute.
+The kernel and the oracle pin the same rounding, so equality is expected
+and checked as well.
+"""
+
+import numpy as np
+import pytest
+
+import oracle
+from pyvr_gb300 import (Camera, ColorTransferFunction, Light, OpacityTransferFunction,
+                        RenderConfig, Volume, VolumeRenderer, compute_normal_volume)
+from pyvr_gb300 import workloads as W
+from pyvr_gb300.renderer import rgba_lut
+
+pytestmark = pytest.mark.gpu
+
+FLOAT_TOL = 1e-6
+
+
+def assert_rgba8_parity(got, want, exact=True):
+    d = np.abs(got.astype(np.int16) - want.astype(np.int16))
+    assert d.max() <= 2, f"max LSB diff {d.max()}"
+    assert (d > 1).mean() <= 1e-3, f"{(d > 1).mean():.2e} of channels off by >1 LSB"
+    if exact:
+        assert d.max() == 0, f"{(d > 0).sum()} channels differ (max {d.max()})"
+
+
+def run_both(vol, cam, light, cfg, ctf, otf, width, height, value_scale=1.0, lut_size=None):
+    lut = rgba_lut(ctf, otf, lut_size)
+    with VolumeRenderer(width, height, config=cfg, light=light) as r:
+        r.load_volume(vol, value_scale=value_scale)
+        r.set_camera(cam)
+        r.set_transfer_functions(ctf, otf, lut_size)
+        g8, gf = r.render_float()
+        gn = r.last_sample_count()
+        b = r.render()
+    assert b == g8.tobytes()  # render() and render_float() give the same bytes
+    s = W.frame_inputs(vol, cam, light, cfg, lut, width, height, value_scale)
+    o8, of, on = oracle.render(s)
+    return g8, gf, gn, o8, of, on
+
+
+def check(vol, cam, light, cfg, ctf, otf, width, height, **kw):
+    g8, gf, gn, o8, of, on = run_both(vol, cam, light, cfg, ctf, otf, width, height, **kw)
+    assert gn == on, (gn, on)
+    assert_rgba8_parity(g8, o8)
+    assert np.abs(gf - of).max() <= FLOAT_TOL
+    return g8, on
+
+
+def test_config_small_exact():
+    c = W.config_small()
+    g8, n = check(c["volume"], c["camera"], c["light"], c["config"], c["ctf"], c["otf"],
+                  c["width"], c["height"])
+    assert n > 1_000_000 and (g8[..., 3] > 0).sum() > 10_000
+
+
+@pytest.mark.parametrize("dtype", ["u8", "f16", "f32"])
+def test_value_noise_dtypes(dtype):
+    noise = W.value_noise((48, 48, 48), seed=11)
+    c = W.config_scale(dtype, n=48, res=96, noise=noise)
+    for k in (0, 5, 11):
+        check(c["volume"], c["cameras"][k], c["light"], c["config"], c["ctf"], c["otf"],
+              96, 96, value_scale=c["value_scale"])
+
+
+def _basic(data, normals=True, bounds=1.0):
+    return Volume(data=data, normals=compute_normal_volume(data) if normals else None,
+                  min_bounds=np.full(3, -bounds, np.float32), max_bounds=np.full(3, bounds, np.float32))
+
+
+CAM = Camera.from_spherical(np.zeros(3, np.float32), 0.9, 0.35, 0.1, 3.0)
+LIGHT = Light.directional([1, -1, 0], 0.2, 0.8)
+CTF = W.standin_colormap(3)
+OTF = OpacityTransferFunction([(0.0, 0.0), (0.3, 0.05), (0.7, 0.25), (1.0, 0.1)])
+
+
+def test_no_normals_uses_density_as_normal():
+    data = W.value_noise((32, 32, 32), seed=2)
+    check(_basic(data, normals=False), CAM, LIGHT, RenderConfig.balanced(), CTF, OTF, 64, 64)
+
+
+def test_noncubic_volume():
+    data = W.value_noise((20, 33, 47), seed=4)
+    check(_basic(data), CAM, LIGHT, RenderConfig.balanced(), CTF, OTF, 80, 60)
+
+
+def test_camera_inside_volume():
+    data = W.value_noise((24, 24, 24), seed=5)
+    cam = Camera.from_spherical(np.zeros(3, np.float32), 0.3, 0.2, 0.0, 0.4)
+    check(_basic(data), cam, LIGHT, RenderConfig.balanced(), CTF, OTF, 48, 48)
+
+
+def test_all_rays_miss():
+    data = W.value_noise((16, 16, 16), seed=6)
+    cam = Camera.from_spherical(np.array([0.0, 0.0, 20.0], np.float32), 0.0, 0.0, 0.0, 3.0)
+    g8, n = check(_basic(data), cam, LIGHT, RenderConfig.balanced(), CTF, OTF, 32, 32)
+    assert n == 0 and not g8.any()
+
+
+def test_single_voxel_and_tiny_image():
+    vol = Volume(data=np.full((1, 1, 1), 0.6, np.float32))
+    check(vol, CAM, LIGHT, RenderConfig.fast(), CTF, OTF, 1, 1)
+    check(vol, CAM, LIGHT, RenderConfig.fast(), CTF, OTF, 37, 23)
+
+
+@pytest.mark.parametrize("lut_size", [1, 2, 255, 5000])
+def test_lut_sizes(lut_size):
+    # 5000 entries exceeds the shared-memory staging limit -> global-memory path
+    data = W.value_noise((24, 24, 24), seed=7)
+    check(_basic(data), CAM, LIGHT, RenderConfig.balanced(), CTF, OTF, 40, 40, lut_size=lut_size)
+
+
+def test_uint8_reference_semantics():
+    # value_scale 1: bytes sample as 0..255 like the reference (saturating the LUT)
+    data = np.rint(W.value_noise((24, 24, 24), seed=8) * 3).astype(np.uint8)
+    check(_basic(data), CAM, LIGHT, RenderConfig.balanced(), CTF, OTF, 40, 40)
+
+
+@pytest.mark.parametrize("light", [Light.ambient_only(0.7), Light.default(),
+                                   Light.point_light(np.array([0.2, 0.1, 0.0]))])
+def test_lights(light):
+    data = W.value_noise((24, 24, 24), seed=9)
+    check(_basic(data), CAM, light, RenderConfig.balanced(), CTF, OTF, 40, 40)
+
+
+@pytest.mark.parametrize("cfg", [RenderConfig.preview(), RenderConfig.ultra_quality(),
+                                 RenderConfig(step_size=0.013, max_steps=1),
+                                 RenderConfig(step_size=0.007, max_steps=37,
+                                              reference_step_size=0.02)])
+def test_configs(cfg):
+    data = W.value_noise((24, 24, 24), seed=10)
+    check(_basic(data), CAM, LIGHT, cfg, CTF, OTF, 40, 32)
+
+
+def test_offset_anisotropic_bounds():
+    data = W.value_noise((16, 24, 32), seed=12)
+    vol = Volume(data=data, normals=compute_normal_volume(data),
+                 min_bounds=np.array([-0.3, -1.2, 0.1], np.float32),
+                 max_bounds=np.array([0.9, 0.4, 0.6], np.float32))
+    check(vol, CAM, LIGHT, RenderConfig.balanced(), CTF, OTF, 50, 70)
+
+
+def test_float64_volume_converted_like_reference():
+    data = W.value_noise((16, 16, 16), seed=13).astype(np.float64)
+    check(_basic(data), CAM, LIGHT, RenderConfig.balanced(), CTF, OTF, 32, 32)
+
+
+def test_render_without_volume_is_transparent():
+    with VolumeRenderer(16, 8) as r:
+        r.set_camera(CAM)
+        b = r.render()
+    assert b == bytes(16 * 8 * 4)
+
+
+def test_render_requires_lut_and_camera():
+    with VolumeRenderer(8, 8) as r:
+        r.load_volume(_basic(np.zeros((4, 4, 4), np.float32)))
+        with pytest.raises(RuntimeError, match="Camera"):
+            r.render()
+        r.set_camera(CAM)
+        with pytest.raises(RuntimeError, match="Transfer functions"):
+            r.render()
+
+
+def test_repeat_and_replace_volume():
+    a = _basic(W.value_noise((20, 20, 20), seed=14))
+    b = _basic(W.value_noise((30, 20, 10), seed=15))
+    with VolumeRenderer(32, 32, light=LIGHT) as r:
+        r.set_camera(CAM)
+        r.set_transfer_functions(CTF, OTF)
+        r.load_volume(a)
+        i1 = r.render()
+        r.load_volume(b)
+        i2 = r.render()
+        r.load_volume(a)
+        i3 = r.render()
+    assert i1 == i3 and i1 != i2
+
+
+def test_scale_config_full_size_rows():
+    """256^3, 1024^2, high_quality: a band of rows against the oracle, for each
+    storage type; the full frame is checked for determinism."""
+    noise = W.config_scale_volume(256)
+    for dtype in ("u8", "f16", "f32"):
+        c = W.config_scale(dtype, noise=noise)
+        cam = c["cameras"][3]
+        lut = rgba_lut(c["ctf"], c["otf"])
+        with VolumeRenderer(1024, 1024, config=c["config"], light=c["light"]) as r:
+            r.load_volume(c["volume"], value_scale=c["value_scale"])
+            r.set_camera(cam)
+            r.set_transfer_functions(c["ctf"], c["otf"])
+            g8, gf = r.render_float()
+            assert r.render() == g8.tobytes()
+        s = W.frame_inputs(c["volume"], cam, c["light"], c["config"], lut, 1024, 1024,
+                           c["value_scale"])
+        rows = (500, 524)
+        o8, of, _ = oracle.render(s, rows=rows)
+        assert_rgba8_parity(g8[rows[0]:rows[1]], o8[rows[0]:rows[1]])
+        assert np.abs(gf[rows[0]:rows[1]] - of[rows[0]:rows[1]]).max() <= FLOAT_TOL
+        assert (g8[..., 3] > 0).mean() > 0.3
