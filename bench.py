@@ -47,6 +47,11 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-rows", type=int, default=256, help="rows per CPU-baseline sample band")
+    # smaller cases for profiling captures
+    ap.add_argument("--storages", default=",".join(DTYPES))
+    ap.add_argument("--cameras", type=int, default=16)
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-e2e", action="store_true")
     return ap.parse_args()
 
 
@@ -121,10 +126,10 @@ def gpu_index(local_rank):
     return local_rank
 
 
-def make_scenes():
+def make_scenes(storages=DTYPES):
     from pyvr_gb300 import workloads as W
     noise = W.config_scale_volume(N_VOL)
-    return {dt: W.config_scale(dt, n=N_VOL, res=RES, noise=noise) for dt in DTYPES}
+    return {dt: W.config_scale(dt, n=N_VOL, res=RES, noise=noise) for dt in storages}
 
 
 def cpu_sample(scenes, rows, nthreads=0, cams=(0, 4, 8, 12)):
@@ -189,9 +194,10 @@ def run_reference(args):
 
 
 def config_dict(args):
+    storages = args.storages.split(",")
     return {"workload": "plain_at_scale", "volume": f"{N_VOL}^3 value noise seed 0",
-            "storages": list(DTYPES), "cameras": 16, "resolution": f"{RES}x{RES}",
-            "render_config": "high_quality", "frames_per_step": 16 * len(DTYPES),
+            "storages": storages, "cameras": args.cameras, "resolution": f"{RES}x{RES}",
+            "render_config": "high_quality", "frames_per_step": args.cameras * len(storages),
             "parallelism": f"replicas x{args.gpus}", "l2": "inputs larger than L2 (208-256 MiB per storage)"}
 
 
@@ -204,7 +210,7 @@ def run_ours(args):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
     from pyvr_gb300 import VolumeRenderer, _native
 
-    scenes = make_scenes()
+    scenes = make_scenes(tuple(args.storages.split(",")))
     lib = _native.load()
     rend = {}
     for dt, c in scenes.items():
@@ -212,18 +218,23 @@ def run_ours(args):
         r.load_volume(c["volume"], value_scale=c["value_scale"])
         r.set_transfer_functions(c["ctf"], c["otf"])
         rend[dt] = r
-    cams = scenes["f32"]["cameras"]
-    stream = torch.cuda.current_stream()
+    cams = next(iter(scenes.values()))["cameras"][:args.cameras]
+    # an explicit stream: handle 0 (the legacy default stream) would mean
+    # "the renderer's own stream" to the C ABI
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sptr = ctypes.c_void_p(stream.cuda_stream)
+    assert sptr.value
     out = torch.empty(RES * RES * 4, dtype=torch.uint8, device="cuda")
 
-    # per-frame in-box sample counts (deterministic), from one counted pass
-    samples = {}
+    # per-frame in-box and shaded sample counts (deterministic), from one
+    # counted pass; the roofline counts the bytes of shaded samples only
+    samples, shaded = {}, {}
     for dt, r in rend.items():
         for k, cam in enumerate(cams):
             r.set_camera(cam)
             _native.check(lib.pvr_render_device(r._h, ctypes.c_void_p(out.data_ptr()), None, sptr))
-            samples[(dt, k)] = r.last_sample_count()
+            samples[(dt, k)], shaded[(dt, k)] = r.last_sample_counts()
 
     def device_step(events=None):
         for dt, r in rend.items():
@@ -261,20 +272,21 @@ def run_ours(args):
     launch_ms = [(dt, k, a.elapsed_time(b)) for dt, k, a, b in events]
 
     # end to end through the public API, host bytes back every frame
-    for _ in range(1):
+    e2e_elapsed = float("nan")
+    if not args.skip_e2e:
         for dt, r in rend.items():
             for cam in cams:
                 r.set_camera(cam)
                 r.render()
-    barrier()
-    te = time.perf_counter()
-    for _ in range(args.steps):
-        for dt, r in rend.items():
-            for cam in cams:
-                r.set_camera(cam)
-                r.render()
-    barrier()
-    e2e_elapsed = time.perf_counter() - te
+        barrier()
+        te = time.perf_counter()
+        for _ in range(args.steps):
+            for dt, r in rend.items():
+                for cam in cams:
+                    r.set_camera(cam)
+                    r.render()
+        barrier()
+        e2e_elapsed = time.perf_counter() - te
 
     frames_per_step = len(rend) * len(cams)
     if world > 1:
@@ -282,24 +294,26 @@ def run_ours(args):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         elapsed, e2e_elapsed = t.tolist()
     value = world * args.steps * frames_per_step / elapsed
-    e2e_value = world * args.steps * frames_per_step / e2e_elapsed
+    e2e_value = (None if args.skip_e2e else
+                 world * args.steps * frames_per_step / e2e_elapsed)
 
     # roofline of the march kernel (algorithmic bytes over event-timed launches)
-    tot_bytes = sum(samples[(dt, k)] * BYTES_PER_SAMPLE[dt] for dt, k, _ in launch_ms)
+    tot_bytes = sum(shaded[(dt, k)] * BYTES_PER_SAMPLE[dt] for dt, k, _ in launch_ms)
     tot_s = sum(ms for _, _, ms in launch_ms) / 1000.0
     achieved = tot_bytes / tot_s / 1e9
     peak, peak_kind = measured_peaks()
     tot_samples = sum(samples[(dt, k)] for dt, k, _ in launch_ms)
     per_dtype = {}
-    for dt in DTYPES:
+    for dt in rend:
         ms = [m for d, _, m in launch_ms if d == dt]
-        by = sum(samples[(d, k)] * BYTES_PER_SAMPLE[d] for d, k, _ in launch_ms if d == dt)
+        by = sum(shaded[(d, k)] * BYTES_PER_SAMPLE[d] for d, k, _ in launch_ms if d == dt)
         per_dtype[dt] = {"avg_launch_ms": statistics.mean(ms),
                          "gbs": by / (sum(ms) / 1000.0) / 1e9,
-                         "samples_per_frame": statistics.mean(samples[(dt, k)] for k in range(len(cams)))}
+                         "samples_per_frame": statistics.mean(samples[(dt, k)] for k in range(len(cams))),
+                         "shaded_per_frame": statistics.mean(shaded[(dt, k)] for k in range(len(cams)))}
 
     cpu = None
-    if rank == 0:
+    if rank == 0 and not args.skip_cpu:
         ct, cn, threads = cpu_sample(scenes, args.cpu_rows)
         mean_frame = statistics.mean(samples.values())
         cpu = {"value": cn / ct / mean_frame, "unit": "renders/s", "cores": threads, "kind": "port",
@@ -318,7 +332,7 @@ def run_ours(args):
                 "samples_per_s": world * args.steps * (tot_samples / args.steps) / elapsed,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
-                             "kernel": "march_linear_kernel", "per_storage": per_dtype},
+                             "kernel": "march_kernel", "per_storage": per_dtype},
                 "cpu_baseline": cpu, "clocks": clk,
                 "e2e": {"value": e2e_value, "unit": "renders/s", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": frames_per_step * RES * RES * 4},

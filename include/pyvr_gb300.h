@@ -105,6 +105,11 @@ int pvr_render_device(pvr_renderer *r, void *d_rgba8, void *d_rgba32f, void *str
  * waits for that render. */
 int pvr_last_sample_count(pvr_renderer *r, long long *samples);
 
+/* Both counters of the most recent render: in-box samples (as above) and the
+ * samples actually fetched and shaded (in-box samples minus those skipped in
+ * bricks that are transparent under the current LUT); waits for that render. */
+int pvr_last_sample_counts(pvr_renderer *r, long long *inbox, long long *shaded);
+
 /* Bytes of device memory this handle holds. */
 int pvr_device_bytes(pvr_renderer *r, long long *bytes);
 

@@ -104,6 +104,7 @@ SIGNATURES = {
     "pvr_render": (_I, [_VP, _VP, _VP]),
     "pvr_render_device": (_I, [_VP, _VP, _VP, _VP]),
     "pvr_last_sample_count": (_I, [_VP, ctypes.POINTER(_LL)]),
+    "pvr_last_sample_counts": (_I, [_VP, ctypes.POINTER(_LL), ctypes.POINTER(_LL)]),
     "pvr_device_bytes": (_I, [_VP, ctypes.POINTER(_LL)]),
 }
 

@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "pvr_device.cuh"
 #include "pvr_internal.h"
@@ -92,10 +93,21 @@ struct pvr_renderer {
     int dims[3] = {0, 0, 0};  // D, H, W
     float value_scale = 1.0f;
     bool has_volume = false;
-    // normals (create_normal_texture)
+    // normals (create_normal_texture); only held until the records are built
     float *d_nrm = nullptr;
     size_t nrm_bytes = 0;
     bool has_normals = false;
+
+    // bricked texel records + brick table + per-brick value range (layout.cu)
+    pvr::BrickGeometry geo = {};
+    float4 *d_records = nullptr;
+    size_t records_bytes = 0;
+    uint32_t *d_table = nullptr;
+    float2 *d_minmax = nullptr;
+    bool layout_dirty = true;
+    bool flags_dirty = true;
+    int *d_prefix = nullptr;  // count of LUT entries that are not exactly transparent
+    int prefix_cap = 0;
     float bmin[3] = {-0.5f, -0.5f, -0.5f}, bmax[3] = {0.5f, 0.5f, 0.5f};
 
     // LUT (create_rgba_transfer_function_texture)
@@ -115,12 +127,26 @@ struct pvr_renderer {
     // render targets
     uint32_t *d_out8 = nullptr;
     float4 *d_outf = nullptr;
-    unsigned long long *d_samples = nullptr;
+    unsigned long long *d_samples = nullptr;  // [in-box samples, shaded samples]
 };
 
 namespace {
 
+void free_layout(pvr_renderer *r) {
+    cudaFree(r->d_records);
+    cudaFree(r->d_table);
+    cudaFree(r->d_minmax);
+    r->d_records = nullptr;
+    r->d_table = nullptr;
+    r->d_minmax = nullptr;
+    r->records_bytes = 0;
+    r->layout_dirty = true;
+}
+
 void free_all(pvr_renderer *r) {
+    free_layout(r);
+    cudaFree(r->d_prefix);
+    r->d_prefix = nullptr;
     cudaFree(r->d_vol);
     cudaFree(r->d_nrm);
     cudaFree(r->d_lut);
@@ -159,12 +185,11 @@ void build_frame(const pvr_renderer *r, pvr::MarchFrame &f) {
         f.inv_ext[a] = 1.0f / (r->bmax[a] - r->bmin[a]);
     }
     // world x <-> texture r (extent W, slowest), y <-> t (H), z <-> s (D)
-    f.ext[0] = r->dims[2];
-    f.ext[1] = r->dims[1];
-    f.ext[2] = r->dims[0];
-    for (int a = 0; a < 3; ++a) f.fext[a] = (float)f.ext[a];
-    f.stride_y = r->dims[0];
-    f.stride_x = (long long)r->dims[0] * r->dims[1];
+    for (int a = 0; a < 3; ++a) {
+        f.ext[a] = r->geo.ext[a];
+        f.fext[a] = (float)f.ext[a];
+        f.nb[a] = r->geo.nb[a];
+    }
     f.step = r->step;
     f.alpha_k = r->step / r->ref_step;
     f.max_steps = r->max_steps;
@@ -184,12 +209,45 @@ int ensure_targets(pvr_renderer *r, bool want_float) {
     size_t npx = (size_t)r->width * r->height;
     if (!r->d_out8) PVR_CUDA(cudaMalloc(&r->d_out8, npx * 4));
     if (want_float && !r->d_outf) PVR_CUDA(cudaMalloc(&r->d_outf, npx * 16));
-    if (!r->d_samples) PVR_CUDA(cudaMalloc(&r->d_samples, sizeof(unsigned long long)));
+    if (!r->d_samples) PVR_CUDA(cudaMalloc(&r->d_samples, 2 * sizeof(unsigned long long)));
+    return PVR_OK;
+}
+
+// Records, brick table and value ranges of the loaded volume (once per
+// volume), then the transparent flags for the current LUT.
+int ensure_layout(pvr_renderer *r) {
+    if (r->layout_dirty) {
+        free_layout(r);
+        r->geo = pvr::make_brick_geometry(r->dims);
+        std::vector<uint32_t> table = pvr::morton_slots(r->geo);
+        size_t nrec = (size_t)r->geo.nbricks * pvr::kRecordsPerBrick;
+        PVR_CUDA(cudaMalloc(&r->d_records, nrec * sizeof(float4)));
+        r->records_bytes = nrec * sizeof(float4);
+        PVR_CUDA(cudaMalloc(&r->d_table, table.size() * sizeof(uint32_t)));
+        PVR_CUDA(cudaMalloc(&r->d_minmax, table.size() * sizeof(float2)));
+        PVR_CUDA(cudaMemcpyAsync(r->d_table, table.data(), table.size() * sizeof(uint32_t),
+                                 cudaMemcpyHostToDevice, r->stream));
+        PVR_CUDA(pvr::launch_build_records(r->geo, r->dtype, r->d_vol,
+                                           r->has_normals ? r->d_nrm : nullptr, r->d_table,
+                                           r->d_records, r->d_minmax, r->stream));
+        PVR_CUDA(cudaStreamSynchronize(r->stream));  // `table` leaves scope
+        cudaFree(r->d_nrm);  // the normals now live in the records
+        r->d_nrm = nullptr;
+        r->nrm_bytes = 0;
+        r->layout_dirty = false;
+        r->flags_dirty = true;
+    }
+    if (r->flags_dirty && r->d_prefix) {
+        bool enable = std::isfinite(r->ambient) && std::isfinite(r->diffuse);
+        PVR_CUDA(pvr::launch_brick_flags(r->geo, r->value_scale, r->lut_size, r->d_prefix, enable,
+                                         r->d_minmax, r->d_table, r->stream));
+        r->flags_dirty = false;
+    }
     return PVR_OK;
 }
 
 int march_into(pvr_renderer *r, uint32_t *d8, float4 *df, cudaStream_t st) {
-    PVR_CUDA(cudaMemsetAsync(r->d_samples, 0, sizeof(unsigned long long), st));
+    PVR_CUDA(cudaMemsetAsync(r->d_samples, 0, 2 * sizeof(unsigned long long), st));
     if (!r->has_volume) {  // unbound samplers read zero: transparent image
         size_t npx = (size_t)r->width * r->height;
         if (d8) PVR_CUDA(cudaMemsetAsync(d8, 0, npx * 4, st));
@@ -201,10 +259,14 @@ int march_into(pvr_renderer *r, uint32_t *d8, float4 *df, cudaStream_t st) {
     if (!r->d_lut)
         return fail(PVR_ERR_STATE,
                     "Transfer functions not set: call set_transfer_functions() before render()");
+    if (int rc = ensure_layout(r)) return rc;
+    if (st != r->stream) {  // layout work was queued on the handle's stream
+        PVR_CUDA(cudaStreamSynchronize(r->stream));
+    }
     pvr::MarchFrame f;
     build_frame(r, f);
-    PVR_CUDA(pvr::launch_march_linear(f, r->dtype, r->d_vol, r->has_normals ? r->d_nrm : nullptr,
-                                      r->d_lut, d8, df, r->d_samples, st));
+    PVR_CUDA(pvr::launch_march(f, r->d_records, r->d_table, r->has_normals, r->d_lut, d8, df,
+                               r->d_samples, st));
     return PVR_OK;
 }
 
@@ -290,12 +352,17 @@ int pvr_load_volume(pvr_renderer *r, const void *data, int dtype, int d, int h, 
     }
     r->has_volume = true;
     r->has_normals = false;
+    cudaFree(r->d_nrm);
+    r->d_nrm = nullptr;
+    r->nrm_bytes = 0;
+    r->layout_dirty = true;
     return PVR_OK;
 }
 
 int pvr_load_normals(pvr_renderer *r, const float *normals) {
     if (int rc = check_handle(r)) return rc;
     if (!normals) {
+        if (r->has_normals) r->layout_dirty = true;
         r->has_normals = false;
         return PVR_OK;
     }
@@ -313,6 +380,7 @@ int pvr_load_normals(pvr_renderer *r, const float *normals) {
     PVR_CUDA(cudaMemcpyAsync(r->d_nrm, normals, bytes, cudaMemcpyHostToDevice, r->stream));
     PVR_CUDA(cudaStreamSynchronize(r->stream));
     r->has_normals = true;
+    r->layout_dirty = true;
     return PVR_OK;
 }
 
@@ -329,10 +397,28 @@ int pvr_set_lut(pvr_renderer *r, const float *rgba, int size) {
         PVR_CUDA(cudaMalloc(&r->d_lut, (size_t)size * sizeof(float4)));
         r->lut_cap = size;
     }
+    if (size + 1 > r->prefix_cap) {
+        cudaFree(r->d_prefix);
+        r->d_prefix = nullptr;
+        r->prefix_cap = 0;
+        PVR_CUDA(cudaMalloc(&r->d_prefix, (size_t)(size + 1) * sizeof(int)));
+        r->prefix_cap = size + 1;
+    }
+    // prefix[i] = entries before i that a skipped sample must not read:
+    // alpha not exactly 0, or a non-finite colour
+    std::vector<int> prefix(size + 1, 0);
+    for (int i = 0; i < size; ++i) {
+        const float *e = rgba + 4 * i;
+        bool clear = e[3] == 0.0f && std::isfinite(e[0]) && std::isfinite(e[1]) && std::isfinite(e[2]);
+        prefix[i + 1] = prefix[i] + (clear ? 0 : 1);
+    }
     PVR_CUDA(cudaMemcpyAsync(r->d_lut, rgba, (size_t)size * sizeof(float4), cudaMemcpyHostToDevice,
                              r->stream));
+    PVR_CUDA(cudaMemcpyAsync(r->d_prefix, prefix.data(), (size_t)(size + 1) * sizeof(int),
+                             cudaMemcpyHostToDevice, r->stream));
     PVR_CUDA(cudaStreamSynchronize(r->stream));
     r->lut_size = size;
+    r->flags_dirty = true;
     return PVR_OK;
 }
 
@@ -360,6 +446,7 @@ int pvr_set_light(pvr_renderer *r, const float position[3], const float target[3
     }
     r->ambient = ambient;
     r->diffuse = diffuse;
+    r->flags_dirty = true;
     return PVR_OK;
 }
 
@@ -410,12 +497,26 @@ int pvr_last_sample_count(pvr_renderer *r, long long *samples) {
     return PVR_OK;
 }
 
+int pvr_last_sample_counts(pvr_renderer *r, long long *inbox, long long *shaded) {
+    if (int rc = check_handle(r)) return rc;
+    if (!inbox || !shaded) return fail(PVR_ERR_VALUE, "output pointer is NULL");
+    DeviceScope ds(r->device);
+    unsigned long long v[2] = {0, 0};
+    PVR_CUDA(cudaDeviceSynchronize());
+    PVR_CUDA(cudaMemcpy(v, r->d_samples, sizeof(v), cudaMemcpyDeviceToHost));
+    *inbox = (long long)v[0];
+    *shaded = (long long)v[1];
+    return PVR_OK;
+}
+
 int pvr_device_bytes(pvr_renderer *r, long long *bytes) {
     if (int rc = check_handle(r)) return rc;
     if (!bytes) return fail(PVR_ERR_VALUE, "bytes is NULL");
     size_t npx = (size_t)r->width * r->height;
-    size_t b = r->vol_bytes + r->nrm_bytes + (size_t)r->lut_cap * sizeof(float4) + npx * 4 +
-               (r->d_outf ? npx * 16 : 0) + sizeof(unsigned long long);
+    size_t b = r->vol_bytes + r->nrm_bytes + r->records_bytes +
+               (size_t)r->geo.nbricks * (sizeof(uint32_t) + sizeof(float2)) +
+               (size_t)r->lut_cap * sizeof(float4) + (size_t)r->prefix_cap * sizeof(int) + npx * 4 +
+               (r->d_outf ? npx * 16 : 0) + 2 * sizeof(unsigned long long);
     *bytes = (long long)b;
     return PVR_OK;
 }

@@ -25,8 +25,7 @@ struct MarchFrame {
     float inv_ext[3];   // 1 / (volume_max_bounds - volume_min_bounds)
     float fext[3];      // texel count along world x, y, z (= W, H, D)
     int ext[3];
-    long long stride_x; // element stride along world x (= D*H) ...
-    long long stride_y; // ... and y (= D); z is contiguous
+    int nb[3];          // bricks along world x, y, z
     float step;         // step_size
     float alpha_k;      // step_size / reference_step_size
     int max_steps;
@@ -64,17 +63,6 @@ __device__ __forceinline__ float pvr_expf(float x) {
     int k1 = k > 0 ? k / 2 : 0;
     int k2 = k - k1;
     return (p * __int_as_float((k1 + 127) << 23)) * __int_as_float((k2 + 127) << 23);
-}
-
-template <typename T> __device__ __forceinline__ float load_voxel(const T *p, long long i);
-template <> __device__ __forceinline__ float load_voxel<float>(const float *p, long long i) {
-    return __ldg(p + i);
-}
-template <> __device__ __forceinline__ float load_voxel<uint8_t>(const uint8_t *p, long long i) {
-    return (float)__ldg(p + i);
-}
-template <> __device__ __forceinline__ float load_voxel<__half>(const __half *p, long long i) {
-    return __half2float(__ldg(p + i));
 }
 
 // Ray of pixel (px, py), py counted from the bottom row: vertex-stage uv at

@@ -213,6 +213,12 @@ class CudaVolumeRenderer:
         check(self._lib.pvr_last_sample_count(self._handle(), ctypes.byref(n)))
         return int(n.value)
 
+    def last_sample_counts(self):
+        """(in-box samples, shaded samples) of the most recent render."""
+        a, b = ctypes.c_longlong(0), ctypes.c_longlong(0)
+        check(self._lib.pvr_last_sample_counts(self._handle(), ctypes.byref(a), ctypes.byref(b)))
+        return int(a.value), int(b.value)
+
     def device_bytes(self) -> int:
         n = ctypes.c_longlong(0)
         check(self._lib.pvr_device_bytes(self._handle(), ctypes.byref(n)))

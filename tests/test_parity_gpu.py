@@ -202,3 +202,47 @@ def test_scale_config_full_size_rows():
         assert_rgba8_parity(g8[rows[0]:rows[1]], o8[rows[0]:rows[1]])
         assert np.abs(gf[rows[0]:rows[1]] - of[rows[0]:rows[1]]).max() <= FLOAT_TOL
         assert (g8[..., 3] > 0).mean() > 0.3
+
+
+def test_empty_space_skipping_is_exact_and_active():
+    # double sphere with opacity linear(0, 0.1): alpha is exactly 0 outside the
+    # spheres, so whole bricks are skipped -- with no change to any output bit
+    c = W.config_small()
+    lut = rgba_lut(c["ctf"], c["otf"])
+    with VolumeRenderer(256, 256, config=c["config"], light=c["light"]) as r:
+        r.load_volume(c["volume"])
+        r.set_camera(c["camera"])
+        r.set_transfer_functions(c["ctf"], c["otf"])
+        g8, gf = r.render_float()
+        inbox, shaded = r.last_sample_counts()
+    o8, of, on = oracle.render(W.frame_inputs(c["volume"], c["camera"], c["light"], c["config"],
+                                              lut, 256, 256))
+    assert inbox == on
+    assert shaded < 0.8 * inbox, (shaded, inbox)
+    assert_rgba8_parity(g8, o8)
+    assert np.abs(gf - of).max() <= FLOAT_TOL
+
+
+def test_lut_change_recomputes_skip_flags():
+    data = W.value_noise((40, 40, 40), seed=21)
+    vol = _basic(data)
+    cfg = RenderConfig.balanced()
+    sparse = OpacityTransferFunction([(0.0, 0.0), (0.6, 0.0), (0.8, 0.3), (1.0, 0.3)])
+    dense = OpacityTransferFunction.linear(0.02, 0.2)
+    with VolumeRenderer(64, 64, config=cfg, light=LIGHT) as r:
+        r.load_volume(vol)
+        r.set_camera(CAM)
+        outs = []
+        for otf in (sparse, dense, sparse):
+            r.set_transfer_functions(CTF, otf)
+            g8, gf = r.render_float()
+            outs.append((otf, g8, gf, r.last_sample_counts()))
+    for otf, g8, gf, (inbox, shaded) in outs:
+        o8, of, on = oracle.render(W.frame_inputs(vol, CAM, LIGHT, cfg, rgba_lut(CTF, otf), 64, 64))
+        assert inbox == on
+        assert_rgba8_parity(g8, o8)
+        assert np.abs(gf - of).max() <= FLOAT_TOL
+    (in0, sh0), (in1, sh1) = outs[0][3], outs[1][3]
+    assert sh0 < in0          # the sparse LUT leaves transparent bricks to skip
+    assert sh1 == in1         # alpha >= 0.02 everywhere: nothing is skipped
+    assert outs[2][3] == outs[0][3]
