@@ -113,6 +113,16 @@ int pvr_last_sample_counts(pvr_renderer *r, long long *inbox, long long *shaded)
 /* Bytes of device memory this handle holds. */
 int pvr_device_bytes(pvr_renderer *r, long long *bytes);
 
+/* Host-only (no CUDA call): the per-frame constants the march derives from
+ * the reference's uniforms (volume.frag.glsl:3-19, 26, 50-52, 101, 107):
+ * out[0..7] rows 0-1 of inverse(projection), out[8..19] rows 0-2 of
+ * inverse(view), out[20..22] normalize(light_target - light_position),
+ * out[23..25] 1/(max_bounds - min_bounds), out[26] step/reference_step. */
+int pvr_frame_constants(const float view[16], const float proj[16], const float light_pos[3],
+                        const float light_target[3], const float min_bounds[3],
+                        const float max_bounds[3], float step_size, float reference_step_size,
+                        float out[27]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -64,6 +64,7 @@ def lib():
                                             ctypes.c_int]
         _lib.oracle_expf_array.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong]
         _lib.oracle_max_threads.restype = ctypes.c_int
+        _lib.oracle_frame_constants.argtypes = [ctypes.POINTER(OracleScene), ctypes.c_void_p]
     return _lib
 
 
@@ -121,6 +122,15 @@ def render(scene: dict, rows=None, want_float: bool = True, nthreads: int = 0,
     if rc != 0:
         raise ValueError("oracle: singular view or projection matrix")
     return out8, outf, (counts if want_counts else int(n.value))
+
+
+def frame_constants(scene: dict) -> np.ndarray:
+    """The 27 derived per-frame floats (see pvr_frame_constants)."""
+    s, keep = make_scene(scene)
+    out = np.zeros(27, dtype=np.float32)
+    if lib().oracle_frame_constants(ctypes.byref(s), out.ctypes.data) != 0:
+        raise ValueError("oracle: singular view or projection matrix")
+    return out
 
 
 def expf(x: np.ndarray) -> np.ndarray:

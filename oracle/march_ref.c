@@ -353,6 +353,18 @@ int oracle_render(const OracleScene *s, uint8_t *out8, float *outf, long long *s
     return oracle_render_rows(s, 0, 0, out8, outf, NULL, samples, nthreads);
 }
 
+/* the derived per-frame constants, in the layout of pvr_frame_constants */
+int oracle_frame_constants(const OracleScene *s, float out[27]) {
+    Derived dv;
+    if (derive(s, &dv)) return -1;
+    memcpy(out, dv.ip, 8 * sizeof(float));
+    memcpy(out + 8, dv.iv, 12 * sizeof(float));
+    memcpy(out + 20, dv.light_dir, 3 * sizeof(float));
+    memcpy(out + 23, dv.inv_ext, 3 * sizeof(float));
+    out[26] = dv.alpha_k;
+    return 0;
+}
+
 /* exposed for tests of the exp restatement */
 void oracle_expf_array(const float *x, float *y, long long n) {
     for (long long i = 0; i < n; ++i) y[i] = oracle_expf(x[i]);

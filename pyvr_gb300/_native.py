@@ -24,8 +24,11 @@ LIB_PATH = os.path.join(PKG, "libpyvr_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # --fmad=false: no implicit multiply-add contraction; the kernels write
 # fmaf() where a fused operation is meant (see csrc/pvr_device.cuh).
+# -ffp-contract=off: the host-side derivations (matrix inverses, light
+# direction) must not be fused into FMAs either -- aarch64 compilers fuse by
+# default, x86-64 ones do not, and the results must not depend on the host.
 NVCC_FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
-              "-Xcompiler", "-fno-fast-math", f"-I{INCLUDE}"]
+              "-Xcompiler", "-fno-fast-math", "-Xcompiler", "-ffp-contract=off", f"-I{INCLUDE}"]
 
 # status codes of include/pyvr_gb300.h
 PVR_OK, PVR_ERR_VALUE, PVR_ERR_TYPE, PVR_ERR_STATE, PVR_ERR_CUDA, PVR_ERR_NOMEM, PVR_ERR_TIMEOUT = range(7)
@@ -106,6 +109,7 @@ SIGNATURES = {
     "pvr_last_sample_count": (_I, [_VP, ctypes.POINTER(_LL)]),
     "pvr_last_sample_counts": (_I, [_VP, ctypes.POINTER(_LL), ctypes.POINTER(_LL)]),
     "pvr_device_bytes": (_I, [_VP, ctypes.POINTER(_LL)]),
+    "pvr_frame_constants": (_I, [_FP, _FP, _FP, _FP, _FP, _FP, _F, _F, _FP]),
 }
 
 

@@ -170,6 +170,14 @@ bool finite3(const float v[3]) {
     return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]);
 }
 
+void light_direction(const float pos[3], const float target[3], float out[3]) {
+    float l[3];
+    for (int a = 0; a < 3; ++a) l[a] = target[a] - pos[a];
+    float l2 = (l[0] * l[0] + l[1] * l[1]) + l[2] * l[2];
+    float li = l2 > 0.0f ? 1.0f / std::sqrt(l2) : 0.0f;
+    for (int a = 0; a < 3; ++a) out[a] = l[a] * li;
+}
+
 // Uniform values -> kernel frame (everything the fragment shader derives
 // per fragment but that is constant over the frame).
 void build_frame(const pvr_renderer *r, pvr::MarchFrame &f) {
@@ -193,11 +201,7 @@ void build_frame(const pvr_renderer *r, pvr::MarchFrame &f) {
     f.step = r->step;
     f.alpha_k = r->step / r->ref_step;
     f.max_steps = r->max_steps;
-    float l[3];
-    for (int a = 0; a < 3; ++a) l[a] = r->light_target[a] - r->light_pos[a];
-    float l2 = (l[0] * l[0] + l[1] * l[1]) + l[2] * l[2];
-    float li = l2 > 0.0f ? 1.0f / std::sqrt(l2) : 0.0f;
-    for (int a = 0; a < 3; ++a) f.light_dir[a] = l[a] * li;
+    light_direction(r->light_pos, r->light_target, f.light_dir);
     f.ambient = r->ambient;
     f.diffuse = r->diffuse;
     f.value_scale = r->value_scale;
@@ -419,6 +423,23 @@ int pvr_set_lut(pvr_renderer *r, const float *rgba, int size) {
     PVR_CUDA(cudaStreamSynchronize(r->stream));
     r->lut_size = size;
     r->flags_dirty = true;
+    return PVR_OK;
+}
+
+int pvr_frame_constants(const float view[16], const float proj[16], const float light_pos[3],
+                        const float light_target[3], const float min_bounds[3],
+                        const float max_bounds[3], float step_size, float reference_step_size,
+                        float out[27]) {
+    if (!view || !proj || !light_pos || !light_target || !min_bounds || !max_bounds || !out)
+        return fail(PVR_ERR_VALUE, "NULL argument");
+    double ip[16], iv[16];
+    if (!invert_gl(proj, ip)) return fail(PVR_ERR_VALUE, "projection matrix is singular");
+    if (!invert_gl(view, iv)) return fail(PVR_ERR_VALUE, "view matrix is singular");
+    for (int i = 0; i < 8; ++i) out[i] = (float)ip[i];
+    for (int i = 0; i < 12; ++i) out[8 + i] = (float)iv[i];
+    light_direction(light_pos, light_target, out + 20);
+    for (int a = 0; a < 3; ++a) out[23 + a] = 1.0f / (max_bounds[a] - min_bounds[a]);
+    out[26] = step_size / reference_step_size;
     return PVR_OK;
 }
 

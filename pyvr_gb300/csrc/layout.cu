@@ -5,10 +5,14 @@
 // once per volume into 16-byte texel records {stored value, nx, ny, nz}
 // (the stored value converted exactly to float; uint8 and float16 keep
 // their values, the scale to density is applied after interpolation),
-// grouped in bricks of kBrick^3 texels plus a one-texel apron on the high
-// side of each axis.  Every trilinear footprint of a sample whose lower
-// texel lies in a brick is then inside that brick's (kBrick+1)^3 records,
-// so one brick base pointer serves all 8 texels of the sample.  Bricks are
+// grouped in bricks of (kBrick+1)^3 records.  The brick grid is shifted by
+// one texel: brick b holds, at local index l, the texel
+// clamp(b*kBrick - 1 + l, 0, extent - 1) on each axis.  A sample with lower
+// texel k = floor(u) in [-1, extent-1] uses brick (k+1)/kBrick and local
+// indices j = (k+1) % kBrick and j+1, which hold exactly the clamp-to-edge
+// texels k0 = clamp(k) and k1 = clamp(k+1) of the GL filter: the clamping
+// is baked into the records, and the 8 texels of a sample sit at fixed
+// offsets from one record address.  Bricks are
 // stored in Morton order of their brick coordinates (a warp's rays walk
 // neighbouring bricks, which then sit in neighbouring memory), located
 // through a brick table whose top bit flags "transparent under the current
@@ -49,9 +53,9 @@ __global__ void build_records_kernel(BrickGeometry g, const T *__restrict__ vol,
         const int by = (brick / g.nb[2]) % g.nb[1];
         const int bx = brick / (g.nb[2] * g.nb[1]);
         const int lz = rec % kApron, ly = (rec / kApron) % kApron, lx = rec / (kApron * kApron);
-        const int x = min(bx * kBrick + lx, g.ext[0] - 1);
-        const int y = min(by * kBrick + ly, g.ext[1] - 1);
-        const int z = min(bz * kBrick + lz, g.ext[2] - 1);
+        const int x = min(max(bx * kBrick - 1 + lx, 0), g.ext[0] - 1);
+        const int y = min(max(by * kBrick - 1 + ly, 0), g.ext[1] - 1);
+        const int z = min(max(bz * kBrick - 1 + lz, 0), g.ext[2] - 1);
         const long long src = z + (long long)g.ext[2] * (y + (long long)g.ext[1] * x);
         float4 v;
         v.x = raw_value<T>(vol, src);
@@ -140,7 +144,8 @@ BrickGeometry make_brick_geometry(const int dims_dhw[3]) {
     g.ext[0] = dims_dhw[2];  // world x <-> W
     g.ext[1] = dims_dhw[1];  // world y <-> H
     g.ext[2] = dims_dhw[0];  // world z <-> D
-    for (int a = 0; a < 3; ++a) g.nb[a] = (g.ext[a] + kBrick - 1) / kBrick;
+    // k + 1 ranges over [0, extent]
+    for (int a = 0; a < 3; ++a) g.nb[a] = g.ext[a] / kBrick + 1;
     g.nbricks = g.nb[0] * g.nb[1] * g.nb[2];
     return g;
 }

@@ -40,6 +40,13 @@ __device__ __forceinline__ float lerp_tex(float a, float b, float t) {
     return fmaf(t, b - a, a);
 }
 
+// Two lerps at once with the packed FP32x2 pipe (sm_100+): per lane the
+// same two IEEE round-to-nearest operations as lerp_tex (b - a is formed
+// exactly as fma(a, -1, b)).
+__device__ __forceinline__ float2 lerp_tex2(float2 a, float2 b, float t) {
+    return __ffma2_rn(make_float2(t, t), __ffma2_rn(a, make_float2(-1.0f, -1.0f), b), a);
+}
+
 // exp(x): k = rint(x/ln2), r = x - k*ln2 with ln2 split 0.693359375 +
 // -2.12194440e-4 (Cody & Waite), exp(r) by its Taylor series to r^7
 // (|r| <= ln2/2, truncation < 0.1 ulp), scaled by 2^k.  Flushes to 0 below

@@ -62,3 +62,45 @@ def test_error_code_mapping():
                       (_native.PVR_ERR_TIMEOUT, TimeoutError)]:
         with pytest.raises(exc):
             _native.check(code)
+
+
+def test_frame_constants_match_oracle_bit_for_bit(native_lib):
+    """The host-side derivations (double inverses, light direction, box
+    reciprocal, step ratio) agree with the oracle's to the bit."""
+    import numpy as np
+
+    import oracle
+    from pyvr_gb300 import Camera, Light, RenderConfig
+    from pyvr_gb300 import workloads as W
+    from pyvr_gb300.renderer import camera_uniforms
+
+    rng = np.random.default_rng(3)
+    lights = [Light.directional([1, -1, 0]), Light.default(), Light.ambient_only(0.3),
+              Light.point_light(np.array([0.3, -2.0, 5.0]))]
+    for i in range(40):
+        cam = Camera.from_spherical(rng.uniform(-0.5, 0.5, 3).astype(np.float32),
+                                    float(rng.uniform(-6, 6)), float(rng.uniform(-1.5, 1.5)),
+                                    float(rng.uniform(-1, 1)), float(rng.uniform(0.5, 6)),
+                                    fov=float(rng.uniform(0.2, 2.5)))
+        w, h = int(rng.integers(1, 2000)), int(rng.integers(1, 2000))
+        view, proj, pos = camera_uniforms(cam, w, h)
+        light = lights[i % len(lights)]
+        bmin = rng.uniform(-2, 0, 3).astype(np.float32)
+        bmax = bmin + rng.uniform(0.1, 3, 3).astype(np.float32)
+        cfg = RenderConfig(step_size=float(rng.uniform(0.001, 0.05)), max_steps=10,
+                           reference_step_size=float(rng.uniform(0.002, 0.03)))
+        lp = np.asarray(light.position, np.float32)
+        lt = np.asarray(light.target, np.float32)
+        got = np.zeros(27, np.float32)
+        f = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+        assert native_lib.pvr_frame_constants(f(view), f(proj), f(lp), f(lt), f(bmin), f(bmax),
+                                              cfg.step_size, cfg.reference_step_size,
+                                              got.ctypes.data_as(ctypes.POINTER(ctypes.c_float))) == 0
+        scene = dict(width=w, height=h, view=view, proj=proj, cam_pos=pos,
+                     volume=np.zeros((2, 2, 2), np.float32), bmin=bmin, bmax=bmax,
+                     lut=np.zeros((1, 4), np.float32), step_size=cfg.step_size,
+                     reference_step_size=cfg.reference_step_size, max_steps=10,
+                     light_pos=lp, light_target=lt, ambient=0.2, diffuse=0.8)
+        want = oracle.frame_constants(scene)
+        # equal values (a structurally zero inverse entry may be +0 or -0)
+        np.testing.assert_array_equal(got, want)

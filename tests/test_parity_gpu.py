@@ -1,9 +1,9 @@
 """GPU parity: the CUDA march through the C ABI against the CPU oracle.
 
 Bar (stated per north-star): RGBA8 within 1 LSB per channel on >= 99.9% of
-pixels and never more than 2 LSB; the float image within 1e-6 absolute.
-The kernel and the oracle pin the same rounding, so equality is expected
-and checked as well.
+pixels and never more than 2 LSB.  The kernel and the oracle pin the same
+rounding, so both the RGBA8 image and the float image are checked for
+equality as well.
 """
 
 import numpy as np
@@ -17,7 +17,7 @@ from pyvr_gb300.renderer import rgba_lut
 
 pytestmark = pytest.mark.gpu
 
-FLOAT_TOL = 1e-6
+FLOAT_TOL = 0.0  # the float image is expected bit-identical too
 
 
 def assert_rgba8_parity(got, want, exact=True):
