@@ -39,7 +39,13 @@ enum pvr_status {
 
 enum pvr_dtype { PVR_U8 = 0, PVR_F16 = 1, PVR_F32 = 2 };
 
+/* normals of a volume resource */
+enum pvr_normals { PVR_NORMALS_NONE = 0, PVR_NORMALS_GIVEN = 1, PVR_NORMALS_DEVICE = 2 };
+
 typedef struct pvr_renderer pvr_renderer;
+typedef struct pvr_volume pvr_volume;
+typedef struct pvr_lut pvr_lut;
+typedef struct pvr_batch pvr_batch;
 
 /* Library identity. */
 int pvr_abi_version(void);
@@ -69,6 +75,14 @@ int pvr_load_volume(pvr_renderer *r, const void *data, int dtype, int d, int h, 
  * them (the march then shades with normalize(density, 0, 0), which is what
  * the reference's unbound normal sampler reads, renderer.py:143-146). */
 int pvr_load_normals(pvr_renderer *r, const float *normals);
+
+/* Volume.compute_normals / compute_normal_volume on the device
+ * (pyvr/volume/data.py:103-118, pyvr/datasets/synthetic.py:109-122) for the
+ * loaded volume: numpy.gradient of the stored values (central inside,
+ * one-sided on faces) / (|g| + 1e-8), in the arithmetic numpy uses for the
+ * storage type (float64 for uint8, float16 for float16, float32 for
+ * float32).  Replaces loaded normals; needs every extent >= 2. */
+int pvr_compute_normals(pvr_renderer *r);
 
 /* set_transfer_functions -> create_rgba_transfer_function_texture
  * (renderer.py:190-207, manager.py:137-186): `rgba` is host float32
@@ -100,6 +114,10 @@ int pvr_render(pvr_renderer *r, uint8_t *out_rgba8, float *out_rgba32f);
  * handle's stream); asynchronous, no host copy.  Either output may be NULL. */
 int pvr_render_device(pvr_renderer *r, void *d_rgba8, void *d_rgba32f, void *stream);
 
+/* Launch shape of this handle's march (see pvr_tuning below). */
+struct pvr_tuning_s;
+int pvr_set_tuning(pvr_renderer *r, const struct pvr_tuning_s *tuning);
+
 /* In-box samples (loop iterations whose texture coordinate is valid,
  * volume.frag.glsl:92) counted by the most recent render on this handle;
  * waits for that render. */
@@ -122,6 +140,72 @@ int pvr_frame_constants(const float view[16], const float proj[16], const float 
                         const float light_target[3], const float min_bounds[3],
                         const float max_bounds[3], float step_size, float reference_step_size,
                         float out[27]);
+
+/* ------------------------------------------------------------------------
+ * Resources and batched rendering (no single reference counterpart: these
+ * split ModernGLManager's per-renderer textures, manager.py:77-186, into
+ * shareable device objects so many renders run in one launch).
+ * ------------------------------------------------------------------------ */
+
+/* A volume on the device: the (D,H,W) voxels of `data` in their own storage
+ * type plus the bricked texel records the march reads (the volume and normal
+ * textures of manager.py:77-135).  normals_mode: PVR_NORMALS_NONE (shade
+ * with normalize(density,0,0)), PVR_NORMALS_GIVEN (`normals` = host float32
+ * (D,H,W,3)), PVR_NORMALS_DEVICE (computed on the device with the semantics
+ * of pyvr/datasets/synthetic.py:109-122 compute_normal_volume, in the
+ * arithmetic numpy uses for the storage type; needs every extent >= 2).
+ * brick_log2: 2, 3 or 4 (bricks of 4^3, 8^3, 16^3 texels), or 0 for the
+ * default 8^3.  Synchronous. */
+int pvr_volume_create(const void *data, int dtype, int d, int h, int w, float value_scale,
+                      const float min_bounds[3], const float max_bounds[3], const float *normals,
+                      int normals_mode, int brick_log2, pvr_volume **out);
+int pvr_volume_destroy(pvr_volume *v);
+int pvr_volume_device_bytes(const pvr_volume *v, long long *bytes);
+/* The float32 (D,H,W,3) normals held in the records (host buffer). */
+int pvr_volume_read_normals(const pvr_volume *v, float *normals_out);
+
+/* The combined RGBA table of create_rgba_transfer_function_texture
+ * (manager.py:137-186) as a device object: host float32 (size, 4). */
+int pvr_lut_create(const float *rgba, int size, pvr_lut **out);
+int pvr_lut_update(pvr_lut *lut, const float *rgba, int size);
+int pvr_lut_destroy(pvr_lut *lut);
+
+/* One render of a batch: the uniforms of renderer.py:148-188, 303-316 plus
+ * its resources and device output buffers. */
+typedef struct {
+    const pvr_volume *volume;
+    const pvr_lut *lut;
+    int width, height;
+    float view[16], proj[16], camera_pos[3];   /* as for pvr_set_camera */
+    float light_pos[3], light_target[3];
+    float ambient, diffuse;
+    float step_size, reference_step_size;
+    int max_steps;
+    void *d_rgba8;                  /* device, width*height*4 bytes, or NULL */
+    void *d_rgba32f;                /* device, width*height*4 floats, or NULL */
+    unsigned long long *d_counters; /* device [in-box, shaded] samples (zeroed by the caller), or NULL */
+} pvr_job;
+
+/* Launch shape of the persistent batch kernel: tile_w x tile_h pixels per
+ * 256-thread block (tile_w a multiple of 8, tile_h of 4, product 256),
+ * march steps per loop iteration (1 or 4), persistent blocks per SM
+ * (0 = as many as fit). */
+typedef struct pvr_tuning_s {
+    int tile_w, tile_h, steps_per_iter, blocks_per_sm;
+} pvr_tuning;
+
+/* A batch launcher with `slots` staging slots (batches that may be in flight
+ * at once).  Each batch is one persistent kernel over a shared work queue of
+ * pixel tiles, launched as a captured CUDA graph. */
+int pvr_batch_create(int capacity_jobs, int slots, pvr_batch **out);
+int pvr_batch_destroy(pvr_batch *b);
+int pvr_batch_set_tuning(pvr_batch *b, const pvr_tuning *tuning);
+int pvr_batch_get_tuning(const pvr_batch *b, pvr_tuning *tuning);
+/* Queue a batch of n jobs on `stream` (NULL = the batch's stream); returns
+ * once it is queued.  All jobs' volumes must share one brick size. */
+int pvr_batch_render(pvr_batch *b, const pvr_job *jobs, int n, void *stream);
+/* Wait for every batch queued on this launcher. */
+int pvr_batch_synchronize(pvr_batch *b);
 
 #ifdef __cplusplus
 }

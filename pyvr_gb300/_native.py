@@ -110,7 +110,38 @@ SIGNATURES = {
     "pvr_last_sample_counts": (_I, [_VP, ctypes.POINTER(_LL), ctypes.POINTER(_LL)]),
     "pvr_device_bytes": (_I, [_VP, ctypes.POINTER(_LL)]),
     "pvr_frame_constants": (_I, [_FP, _FP, _FP, _FP, _FP, _FP, _F, _F, _FP]),
+    "pvr_compute_normals": (_I, [_VP]),
+    "pvr_set_tuning": (_I, [_VP, _VP]),
+    "pvr_volume_create": (_I, [_VP, _I, _I, _I, _I, _F, _FP, _FP, _VP, _I, _I, ctypes.POINTER(_VP)]),
+    "pvr_volume_destroy": (_I, [_VP]),
+    "pvr_volume_device_bytes": (_I, [_VP, ctypes.POINTER(_LL)]),
+    "pvr_volume_read_normals": (_I, [_VP, _VP]),
+    "pvr_lut_create": (_I, [_VP, _I, ctypes.POINTER(_VP)]),
+    "pvr_lut_update": (_I, [_VP, _VP, _I]),
+    "pvr_lut_destroy": (_I, [_VP]),
+    "pvr_batch_create": (_I, [_I, _I, ctypes.POINTER(_VP)]),
+    "pvr_batch_destroy": (_I, [_VP]),
+    "pvr_batch_set_tuning": (_I, [_VP, _VP]),
+    "pvr_batch_get_tuning": (_I, [_VP, _VP]),
+    "pvr_batch_render": (_I, [_VP, _VP, _I, _VP]),
+    "pvr_batch_synchronize": (_I, [_VP]),
 }
+
+PVR_NORMALS_NONE, PVR_NORMALS_GIVEN, PVR_NORMALS_DEVICE = 0, 1, 2
+
+
+class PvrTuning(ctypes.Structure):
+    """pvr_tuning of include/pyvr_gb300.h."""
+    _fields_ = [("tile_w", _I), ("tile_h", _I), ("steps_per_iter", _I), ("blocks_per_sm", _I)]
+
+
+class PvrJob(ctypes.Structure):
+    """pvr_job of include/pyvr_gb300.h."""
+    _fields_ = [("volume", _VP), ("lut", _VP), ("width", _I), ("height", _I),
+                ("view", _F * 16), ("proj", _F * 16), ("camera_pos", _F * 3),
+                ("light_pos", _F * 3), ("light_target", _F * 3), ("ambient", _F), ("diffuse", _F),
+                ("step_size", _F), ("reference_step_size", _F), ("max_steps", _I),
+                ("d_rgba8", _VP), ("d_rgba32f", _VP), ("d_counters", _VP)]
 
 
 def load(path: str = LIB_PATH, build_if_missing: bool = True):

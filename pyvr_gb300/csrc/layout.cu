@@ -5,18 +5,18 @@
 // once per volume into 16-byte texel records {stored value, nx, ny, nz}
 // (the stored value converted exactly to float; uint8 and float16 keep
 // their values, the scale to density is applied after interpolation),
-// grouped in bricks of (kBrick+1)^3 records.  The brick grid is shifted by
-// one texel: brick b holds, at local index l, the texel
-// clamp(b*kBrick - 1 + l, 0, extent - 1) on each axis.  A sample with lower
-// texel k = floor(u) in [-1, extent-1] uses brick (k+1)/kBrick and local
-// indices j = (k+1) % kBrick and j+1, which hold exactly the clamp-to-edge
-// texels k0 = clamp(k) and k1 = clamp(k+1) of the GL filter: the clamping
-// is baked into the records, and the 8 texels of a sample sit at fixed
-// offsets from one record address.  Bricks are
-// stored in Morton order of their brick coordinates (a warp's rays walk
-// neighbouring bricks, which then sit in neighbouring memory), located
-// through a brick table whose top bit flags "transparent under the current
-// LUT" for empty-space skipping.
+// grouped in bricks of (B+1)^3 records for bricks of B^3 texels.  The
+// brick grid is shifted by one texel: brick b holds, at local index l, the
+// texel clamp(b*B - 1 + l, 0, extent - 1) on each axis.  A sample with
+// lower texel k = floor(u) in [-1, extent-1] uses brick (k+1)/B and local
+// indices j = (k+1) % B and j+1, which hold exactly the clamp-to-edge texels
+// clamp(k) and clamp(k+1) of the GL filter: the clamping is baked into the
+// records, and the 8 texels of a sample sit at fixed offsets from one
+// record address.  Bricks are stored in Morton order of their brick
+// coordinates (a warp's rays walk neighbouring bricks, which then sit in
+// neighbouring memory), located through a brick table.  A per-brick
+// min/max of the stored values lets the march skip bricks that the current
+// LUT makes exactly transparent.
 #include <algorithm>
 #include <vector>
 
@@ -36,53 +36,150 @@ template <> __device__ __forceinline__ float raw_value<__half>(const __half *p, 
     return __half2float(p[i]);
 }
 
+__device__ __forceinline__ float round_half(float x) { return __half2float(__float2half_rn(x)); }
+
+// Normal of array element (a, b, c) of the (D,H,W) volume, as
+// pyvr/datasets/synthetic.py:109-122 computes it with numpy:
+// g_axis = numpy.gradient along each array axis (central difference / 2
+// inside, one-sided on the two faces, unit spacing), n = |g| + 1e-8 with
+// the squares summed left to right, normal = g / n, cast to float32.
+// numpy evaluates this in float64 for integer input, in float16 (each
+// operation rounded to half, sums accumulated in float) for float16 input,
+// and in float32 for float32 input; so does this function.
+template <typename T> struct GradientArith;
+
+template <> struct GradientArith<float> {
+    static __device__ float3 normal(const float *v, const int dims[3], int a, int b, int c) {
+        float g[3];
+        const int idx[3] = {a, b, c};
+        const long long stride[3] = {(long long)dims[1] * dims[2], dims[2], 1};
+        const long long base = a * stride[0] + b * stride[1] + c;
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+            const int i = idx[ax], n = dims[ax];
+            const long long s = stride[ax];
+            if (i == 0) g[ax] = __fsub_rn(v[base + s], v[base]);
+            else if (i == n - 1) g[ax] = __fsub_rn(v[base], v[base - s]);
+            else g[ax] = __fmul_rn(__fsub_rn(v[base + s], v[base - s]), 0.5f);
+        }
+        float ss = __fadd_rn(__fadd_rn(__fmul_rn(g[0], g[0]), __fmul_rn(g[1], g[1])), __fmul_rn(g[2], g[2]));
+        float nrm = __fadd_rn(__fsqrt_rn(ss), 1e-8f);
+        return make_float3(__fdiv_rn(g[0], nrm), __fdiv_rn(g[1], nrm), __fdiv_rn(g[2], nrm));
+    }
+};
+
+template <> struct GradientArith<uint8_t> {
+    static __device__ float3 normal(const uint8_t *v, const int dims[3], int a, int b, int c) {
+        double g[3];
+        const int idx[3] = {a, b, c};
+        const long long stride[3] = {(long long)dims[1] * dims[2], dims[2], 1};
+        const long long base = a * stride[0] + b * stride[1] + c;
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+            const int i = idx[ax], n = dims[ax];
+            const long long s = stride[ax];
+            if (i == 0) g[ax] = (double)v[base + s] - (double)v[base];
+            else if (i == n - 1) g[ax] = (double)v[base] - (double)v[base - s];
+            else g[ax] = ((double)v[base + s] - (double)v[base - s]) / 2.0;  // exact
+        }
+        double ss = __dadd_rn(__dadd_rn(__dmul_rn(g[0], g[0]), __dmul_rn(g[1], g[1])), __dmul_rn(g[2], g[2]));
+        double nrm = __dadd_rn(__dsqrt_rn(ss), 1e-8);
+        return make_float3(__double2float_rn(__ddiv_rn(g[0], nrm)), __double2float_rn(__ddiv_rn(g[1], nrm)),
+                           __double2float_rn(__ddiv_rn(g[2], nrm)));
+    }
+};
+
+template <> struct GradientArith<__half> {
+    static __device__ float3 normal(const __half *v, const int dims[3], int a, int b, int c) {
+        float g[3];
+        const int idx[3] = {a, b, c};
+        const long long stride[3] = {(long long)dims[1] * dims[2], dims[2], 1};
+        const long long base = a * stride[0] + b * stride[1] + c;
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+            const int i = idx[ax], n = dims[ax];
+            const long long s = stride[ax];
+            if (i == 0) {
+                g[ax] = round_half(__fsub_rn(__half2float(v[base + s]), __half2float(v[base])));
+            } else if (i == n - 1) {
+                g[ax] = round_half(__fsub_rn(__half2float(v[base]), __half2float(v[base - s])));
+            } else {
+                float d = round_half(__fsub_rn(__half2float(v[base + s]), __half2float(v[base - s])));
+                g[ax] = round_half(__fdiv_rn(d, 2.0f));
+            }
+        }
+        // squares rounded to half; the sum accumulates in float, rounds once
+        float q0 = round_half(__fmul_rn(g[0], g[0]));
+        float q1 = round_half(__fmul_rn(g[1], g[1]));
+        float q2 = round_half(__fmul_rn(g[2], g[2]));
+        float ss = round_half(__fadd_rn(__fadd_rn(q0, q1), q2));
+        float nrm = round_half(__fsqrt_rn(ss));  // + 1e-8 rounds to + 0 in half
+        return make_float3(round_half(__fdiv_rn(g[0], nrm)), round_half(__fdiv_rn(g[1], nrm)),
+                           round_half(__fdiv_rn(g[2], nrm)));
+    }
+};
+
 // One thread per record.  Voxel (x, y, z) along world axes lives at
 // z + D*(y + H*x) of the (D,H,W) C-order buffer (the GL texture of size
-// (D,H,W) read through the z/y/x swizzle, volume.frag.glsl:90).
-template <typename T>
-__global__ void build_records_kernel(BrickGeometry g, const T *__restrict__ vol,
-                                     const float *__restrict__ nrm,
+// (D,H,W) read through the z/y/x swizzle, volume.frag.glsl:90); the normal
+// texture is indexed the same way (manager.py:123-125).
+template <typename T, int LOG2B>
+__global__ void build_records_kernel(BrickGeometry g, const T *__restrict__ vol, int D, int H, int W,
+                                     const float *__restrict__ nrm, int normals_mode,
                                      const uint32_t *__restrict__ table,
                                      float4 *__restrict__ records) {
-    const long long total = (long long)g.nbricks * kRecordsPerBrick;
+    constexpr int B = 1 << LOG2B, A = B + 1, R = A * A * A;
+    const int dims[3] = {D, H, W};
+    const long long total = (long long)g.nbricks * R;
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < total;
          r += (long long)gridDim.x * blockDim.x) {
-        const int brick = (int)(r / kRecordsPerBrick);
-        const int rec = (int)(r - (long long)brick * kRecordsPerBrick);
+        const int brick = (int)(r / R);
+        const int rec = (int)(r - (long long)brick * R);
         const int bz = brick % g.nb[2];
         const int by = (brick / g.nb[2]) % g.nb[1];
         const int bx = brick / (g.nb[2] * g.nb[1]);
-        const int lz = rec % kApron, ly = (rec / kApron) % kApron, lx = rec / (kApron * kApron);
-        const int x = min(max(bx * kBrick - 1 + lx, 0), g.ext[0] - 1);
-        const int y = min(max(by * kBrick - 1 + ly, 0), g.ext[1] - 1);
-        const int z = min(max(bz * kBrick - 1 + lz, 0), g.ext[2] - 1);
+        const int lz = rec % A, ly = (rec / A) % A, lx = rec / (A * A);
+        const int x = min(max(bx * B - 1 + lx, 0), g.ext[0] - 1);
+        const int y = min(max(by * B - 1 + ly, 0), g.ext[1] - 1);
+        const int z = min(max(bz * B - 1 + lz, 0), g.ext[2] - 1);
         const long long src = z + (long long)g.ext[2] * (y + (long long)g.ext[1] * x);
         float4 v;
         v.x = raw_value<T>(vol, src);
-        if (nrm) {
+        if (normals_mode == PVR_NORMALS_GIVEN) {
             v.y = nrm[3 * src + 0];
             v.z = nrm[3 * src + 1];
             v.w = nrm[3 * src + 2];
+        } else if (normals_mode == PVR_NORMALS_DEVICE) {
+            // array position of flat element `src` in the (D,H,W) array
+            const int c = (int)(src % W);
+            const int b = (int)((src / W) % H);
+            const int a = (int)(src / ((long long)W * H));
+            const float3 n = GradientArith<T>::normal(vol, dims, a, b, c);
+            v.y = n.x;
+            v.z = n.y;
+            v.w = n.z;
         } else {
             v.y = v.z = v.w = 0.0f;
         }
-        const uint32_t slot = table[brick] & kSlotMask;
-        records[(size_t)slot * kRecordsPerBrick + rec] = v;
+        const uint32_t slot = table[brick];
+        records[(size_t)slot * R + rec] = v;
     }
 }
 
 // One warp per brick: min/max of the stored values over all its records
 // (the footprints of every sample that maps to it).  A NaN marks the brick
 // as never skippable.
+template <int LOG2B>
 __global__ void brick_minmax_kernel(BrickGeometry g, const uint32_t *__restrict__ table,
                                     const float4 *__restrict__ records, float2 *__restrict__ mm) {
+    constexpr int R = brick_records(LOG2B);
     const int warps = blockDim.x >> 5;
     const int lane = threadIdx.x & 31;
     for (int b = blockIdx.x * warps + (threadIdx.x >> 5); b < g.nbricks; b += gridDim.x * warps) {
-        const float4 *rp = records + (size_t)(table[b] & kSlotMask) * kRecordsPerBrick;
+        const float4 *rp = records + (size_t)table[b] * R;
         float lo = __int_as_float(0x7f800000), hi = -lo;
         bool nan = false;
-        for (int i = lane; i < kRecordsPerBrick; i += 32) {
+        for (int i = lane; i < R; i += 32) {
             float v = rp[i].x;
             nan |= v != v;
             lo = fminf(lo, v);
@@ -98,33 +195,27 @@ __global__ void brick_minmax_kernel(BrickGeometry g, const uint32_t *__restrict_
     }
 }
 
-// Transparent flag of each brick for one LUT: every LUT entry that a sample
-// of the brick can read has alpha exactly 0 and a finite colour.  Such a
-// sample adds exactly +0 to every accumulator (volume.frag.glsl:101-115), so
-// skipping it changes no bit of the result.  The entry range is exact, not
-// padded: a lerp fmaf(t, b - a, a) with t in [0, 1) never leaves
-// [min(a,b), max(a,b)], so a trilinear sample lies in the brick's value
-// range, and the scale and the LUT coordinate d*size - 0.5 are monotone
-// float operations evaluated here exactly as the march kernel does.
-__global__ void brick_flags_kernel(BrickGeometry g, float value_scale, int lut_size,
-                                   const int *__restrict__ opaque_prefix, int enable,
-                                   const float2 *__restrict__ mm, uint32_t *__restrict__ table) {
-    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < g.nbricks; b += gridDim.x * blockDim.x) {
-        float2 m = mm[b];
-        bool transparent = false;
-        if (enable && m.x == m.x) {
-            float d0 = m.x * value_scale, d1 = m.y * value_scale;
-            float dlo = fminf(d0, d1), dhi = fmaxf(d0, d1);
-            float flo = floorf(dlo * (float)lut_size - 0.5f);
-            float fhi = floorf(dhi * (float)lut_size - 0.5f) + 1.0f;
-            float fmax_idx = (float)(lut_size - 1);
-            int ilo = !(flo >= 0.0f) ? 0 : (flo > fmax_idx ? lut_size - 1 : (int)flo);
-            int ihi = !(fhi >= 0.0f) ? 0 : (fhi > fmax_idx ? lut_size - 1 : (int)fhi);
-            if (dlo == dlo && dhi == dhi)  // finite range (inf*0 etc. excluded)
-                transparent = opaque_prefix[ihi + 1] - opaque_prefix[ilo] == 0;
-        }
-        uint32_t e = table[b] & kSlotMask;
-        table[b] = transparent ? (e | kTransparentBit) : e;
+// Scatter the normals held in the records back to (D,H,W,3): one thread per
+// texel, reading the record of local index (k+1) % B in brick (k+1) / B.
+template <int LOG2B>
+__global__ void read_normals_kernel(BrickGeometry g, int D, int H, int W,
+                                    const uint32_t *__restrict__ table,
+                                    const float4 *__restrict__ records, float *__restrict__ out) {
+    constexpr int B = 1 << LOG2B, A = B + 1, R = A * A * A;
+    const long long total = (long long)D * H * W;
+    for (long long src = blockIdx.x * (long long)blockDim.x + threadIdx.x; src < total;
+         src += (long long)gridDim.x * blockDim.x) {
+        // flat texel index src = z + D*(y + H*x) (world axes)
+        const int z = (int)(src % D);
+        const int y = (int)((src / D) % H);
+        const int x = (int)(src / ((long long)D * H));
+        const int kx = x + 1, ky = y + 1, kz = z + 1;
+        const int id = ((kx >> LOG2B) * g.nb[1] + (ky >> LOG2B)) * g.nb[2] + (kz >> LOG2B);
+        const int rec = ((kx & (B - 1)) * A + (ky & (B - 1))) * A + (kz & (B - 1));
+        const float4 v = records[(size_t)table[id] * R + rec];
+        out[3 * src + 0] = v.y;
+        out[3 * src + 1] = v.z;
+        out[3 * src + 2] = v.w;
     }
 }
 
@@ -137,15 +228,46 @@ uint32_t spread3(uint32_t v) {  // 10 bits -> every third bit
     return v;
 }
 
+template <typename T, int LOG2B>
+cudaError_t build_typed(const BrickGeometry &g, const void *vol, const int dims[3], const float *nrm,
+                        int normals_mode, const uint32_t *table, float4 *records, float2 *minmax,
+                        cudaStream_t st) {
+    constexpr int R = brick_records(LOG2B);
+    const long long total = (long long)g.nbricks * R;
+    int blocks = (int)std::min<long long>((total + 255) / 256, 152LL * 64);
+    build_records_kernel<T, LOG2B><<<blocks, 256, 0, st>>>(g, (const T *)vol, dims[0], dims[1], dims[2],
+                                                          nrm, normals_mode, table, records);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    int mblocks = std::max(1, std::min((g.nbricks + 7) / 8, 152 * 16));
+    brick_minmax_kernel<LOG2B><<<mblocks, 256, 0, st>>>(g, table, records, minmax);
+    return cudaGetLastError();
+}
+
+template <int LOG2B>
+cudaError_t build_log2(const BrickGeometry &g, int dtype, const void *vol, const int dims[3],
+                       const float *nrm, int normals_mode, const uint32_t *table, float4 *records,
+                       float2 *minmax, cudaStream_t st) {
+    switch (dtype) {
+    case PVR_U8:
+        return build_typed<uint8_t, LOG2B>(g, vol, dims, nrm, normals_mode, table, records, minmax, st);
+    case PVR_F16:
+        return build_typed<__half, LOG2B>(g, vol, dims, nrm, normals_mode, table, records, minmax, st);
+    default:
+        return build_typed<float, LOG2B>(g, vol, dims, nrm, normals_mode, table, records, minmax, st);
+    }
+}
+
 }  // namespace
 
-BrickGeometry make_brick_geometry(const int dims_dhw[3]) {
+BrickGeometry make_brick_geometry(const int dims_dhw[3], int log2b) {
     BrickGeometry g;
+    g.log2b = log2b;
     g.ext[0] = dims_dhw[2];  // world x <-> W
     g.ext[1] = dims_dhw[1];  // world y <-> H
     g.ext[2] = dims_dhw[0];  // world z <-> D
     // k + 1 ranges over [0, extent]
-    for (int a = 0; a < 3; ++a) g.nb[a] = g.ext[a] / kBrick + 1;
+    for (int a = 0; a < 3; ++a) g.nb[a] = (g.ext[a] >> log2b) + 1;
     g.nbricks = g.nb[0] * g.nb[1] * g.nb[2];
     return g;
 }
@@ -166,34 +288,25 @@ std::vector<uint32_t> morton_slots(const BrickGeometry &g) {
     return table;
 }
 
-cudaError_t launch_build_records(const BrickGeometry &g, int dtype, const void *vol, const float *nrm,
-                                 const uint32_t *table, float4 *records, float2 *minmax,
-                                 cudaStream_t st) {
-    const long long total = (long long)g.nbricks * kRecordsPerBrick;
-    int blocks = (int)std::min<long long>((total + 255) / 256, 152LL * 64);
-    switch (dtype) {
-    case PVR_U8:
-        build_records_kernel<uint8_t><<<blocks, 256, 0, st>>>(g, (const uint8_t *)vol, nrm, table, records);
-        break;
-    case PVR_F16:
-        build_records_kernel<__half><<<blocks, 256, 0, st>>>(g, (const __half *)vol, nrm, table, records);
-        break;
-    default:
-        build_records_kernel<float><<<blocks, 256, 0, st>>>(g, (const float *)vol, nrm, table, records);
+cudaError_t launch_build_records(const BrickGeometry &g, int dtype, const void *vol, const int dims[3],
+                                 const float *nrm, int normals_mode, const uint32_t *table,
+                                 float4 *records, float2 *minmax, cudaStream_t st) {
+    switch (g.log2b) {
+    case 2: return build_log2<2>(g, dtype, vol, dims, nrm, normals_mode, table, records, minmax, st);
+    case 4: return build_log2<4>(g, dtype, vol, dims, nrm, normals_mode, table, records, minmax, st);
+    default: return build_log2<3>(g, dtype, vol, dims, nrm, normals_mode, table, records, minmax, st);
     }
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    int mblocks = std::max(1, std::min((g.nbricks + 7) / 8, 152 * 16));
-    brick_minmax_kernel<<<mblocks, 256, 0, st>>>(g, table, records, minmax);
-    return cudaGetLastError();
 }
 
-cudaError_t launch_brick_flags(const BrickGeometry &g, float value_scale, int lut_size,
-                               const int *opaque_prefix, bool enable, const float2 *minmax,
-                               uint32_t *table, cudaStream_t st) {
-    int blocks = std::max(1, std::min((g.nbricks + 255) / 256, 152 * 8));
-    brick_flags_kernel<<<blocks, 256, 0, st>>>(g, value_scale, lut_size, opaque_prefix, enable ? 1 : 0,
-                                               minmax, table);
+cudaError_t launch_read_normals(const BrickGeometry &g, const int dims[3], const uint32_t *table,
+                                const float4 *records, float *out, cudaStream_t st) {
+    const long long total = (long long)dims[0] * dims[1] * dims[2];
+    int blocks = (int)std::min<long long>((total + 255) / 256, 152LL * 64);
+    switch (g.log2b) {
+    case 2: read_normals_kernel<2><<<blocks, 256, 0, st>>>(g, dims[0], dims[1], dims[2], table, records, out); break;
+    case 4: read_normals_kernel<4><<<blocks, 256, 0, st>>>(g, dims[0], dims[1], dims[2], table, records, out); break;
+    default: read_normals_kernel<3><<<blocks, 256, 0, st>>>(g, dims[0], dims[1], dims[2], table, records, out);
+    }
     return cudaGetLastError();
 }
 

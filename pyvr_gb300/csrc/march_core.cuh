@@ -1,0 +1,353 @@
+// The ray-march kernel: pyvr/shaders/volume.frag.glsl:main as CUDA, run as
+// a persistent kernel over a batch of renders.
+//
+// Work is a queue of pixel tiles over every job of the batch (one job =
+// one render with its own volume, LUT, camera, light, config and size).
+// Each 256-thread block pops a tile with one atomic, caches the tile's job
+// descriptor in shared memory when the job changes and stages that job's
+// RGBA LUT (plus the LUT's "clear entry" prefix counts) next to it, then
+// marches one ray per thread.  Warps cover 8x4-pixel sub-tiles so the rays
+// of a warp are spatially close and their trilinear footprints share cache
+// lines.  Voxels and normals are read from the bricked 16-byte texel
+// records of layout.cu: each sample is 8 vector loads at fixed offsets from
+// one record address.  Paired channels go through the packed FP32x2 pipe,
+// which rounds each lane exactly like the scalar instruction; an add that
+// consumes a packed product is always a scalar __fadd_rn, so no
+// product/add pair can be fused into one rounding.
+//
+// The march reproduces the reference loop (frag:87-119) exactly, with two
+// shortcuts that change no output bit:
+//  - the ray's texture coordinate is monotone in the step index along each
+//    axis (the position advances by repeated addition of one float step),
+//    so the steps whose coordinate is valid (frag:92) form one contiguous
+//    run; once the ray has left it, or provably cannot enter it, every
+//    remaining iteration would be a no-op and the loop ends;
+//  - a sample in a brick whose value range maps only to LUT entries with
+//    alpha exactly 0 (and a finite colour) adds exactly +0 to every
+//    accumulator, so its fetches and shading are skipped; the position
+//    still advances by the same float additions.  The LUT entry range is
+//    exact: a lerp fmaf(t, b-a, a) with t in [0,1) stays within [a, b], so
+//    a sample lies in the brick's value range, and the scale and the LUT
+//    coordinate are monotone float operations evaluated as for a sample.
+#pragma once
+
+#include "pvr_device.cuh"
+#include "pvr_internal.h"
+
+namespace pvr {
+
+__device__ __forceinline__ float2 lo2(float4 v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z, v.w); }
+__device__ __forceinline__ float2 dup2(float v) { return make_float2(v, v); }
+
+template <bool SMEM>
+__device__ __forceinline__ float4 lut_entry(const float4 *lut, int i) {
+    if (SMEM) return lut[i];
+    return __ldg(lut + i);
+}
+template <bool SMEM>
+__device__ __forceinline__ int prefix_entry(const int *p, int i) {
+    if (SMEM) return p[i];
+    return __ldg(p + i);
+}
+
+// LUT entry index of density d: floor(d*size - 0.5) clamped to the table,
+// as texture(transfer_function_lut, vec2(d, 0.5)) addresses it (frag:96).
+__device__ __forceinline__ int lut_index(float fl, float lmax, int size) {
+    return !(fl >= 0.0f) ? 0 : (fl > lmax ? size - 1 : (int)fl);
+}
+
+// Shading + compositing of one in-box sample (frag:93-115).  p: the record
+// of the footprint's lower corner; fx, fy, fz: the filter fractions.
+template <int LOG2B, bool NORMALS, bool SMEM_LUT>
+__device__ __forceinline__ void shade_sample(const MarchFrame &f, const float4 *__restrict__ p,
+                                             float fx, float fy, float fz, const float4 *lut,
+                                             float2 &acc_rg, float2 &acc_ba) {
+    constexpr int ROW = brick_apron(LOG2B), SLICE = ROW * ROW;
+    float density;
+    float n[3];
+    if (NORMALS) {
+        const float4 r000 = __ldg(p);
+        const float4 r001 = __ldg(p + 1);
+        const float4 r010 = __ldg(p + ROW);
+        const float4 r011 = __ldg(p + ROW + 1);
+        const float4 r100 = __ldg(p + SLICE);
+        const float4 r101 = __ldg(p + SLICE + 1);
+        const float4 r110 = __ldg(p + SLICE + ROW);
+        const float4 r111 = __ldg(p + SLICE + ROW + 1);
+        // texture(volume_texture, tex.zyx) and texture(normal_volume, ...):
+        // lerp along z, then y, then x; lanes (value, nx) and (ny, nz)
+        const float2 a = lerp_tex2(lerp_tex2(lerp_tex2(lo2(r000), lo2(r001), fz),
+                                             lerp_tex2(lo2(r010), lo2(r011), fz), fy),
+                                   lerp_tex2(lerp_tex2(lo2(r100), lo2(r101), fz),
+                                             lerp_tex2(lo2(r110), lo2(r111), fz), fy), fx);
+        const float2 b = lerp_tex2(lerp_tex2(lerp_tex2(hi2(r000), hi2(r001), fz),
+                                             lerp_tex2(hi2(r010), hi2(r011), fz), fy),
+                                   lerp_tex2(lerp_tex2(hi2(r100), hi2(r101), fz),
+                                             lerp_tex2(hi2(r110), hi2(r111), fz), fy), fx);
+        density = __fmul_rn(a.x, f.value_scale);
+        n[0] = a.y;
+        n[1] = b.x;
+        n[2] = b.y;
+    } else {
+        const float *q = reinterpret_cast<const float *>(p);
+        const float v000 = __ldg(q), v001 = __ldg(q + 4);
+        const float v010 = __ldg(q + 4 * ROW), v011 = __ldg(q + 4 * ROW + 4);
+        const float v100 = __ldg(q + 4 * SLICE), v101 = __ldg(q + 4 * SLICE + 4);
+        const float v110 = __ldg(q + 4 * (SLICE + ROW)), v111 = __ldg(q + 4 * (SLICE + ROW) + 4);
+        const float2 zz0 = lerp_tex2(make_float2(v000, v010), make_float2(v001, v011), fz);
+        const float2 zz1 = lerp_tex2(make_float2(v100, v110), make_float2(v101, v111), fz);
+        const float2 yy = lerp_tex2(make_float2(zz0.x, zz1.x), make_float2(zz0.y, zz1.y), fy);
+        density = __fmul_rn(lerp_tex(yy.x, yy.y, fx), f.value_scale);
+        // the reference's unbound normal sampler reads the R32F volume
+        // texture: normal = (density, 0, 0)
+        n[0] = density;
+        n[1] = 0.0f;
+        n[2] = 0.0f;
+    }
+
+    // texture(transfer_function_lut, vec2(density, 0.5)) (frag:96)
+    const float lu = __fadd_rn(__fmul_rn(density, f.flut_size), -0.5f);
+    const float lfl = floorf(lu);
+    const float la = __fadd_rn(lu, -lfl);
+    const float lmax = (float)(f.lut_size - 1);
+    const int i0 = lut_index(lfl, lmax, f.lut_size);
+    const int i1 = lut_index(__fadd_rn(lfl, 1.0f), lmax, f.lut_size);
+    const float4 A = lut_entry<SMEM_LUT>(lut, i0), B = lut_entry<SMEM_LUT>(lut, i1);
+    const float2 crg = lerp_tex2(lo2(A), lo2(B), la);
+    const float2 cba = lerp_tex2(hi2(A), hi2(B), la);  // (blue, alpha_tf)
+
+    // Beer-Lambert opacity correction (frag:101)
+    const float alpha = __fadd_rn(1.0f, -pvr_expf(-__fmul_rn(cba.y, f.alpha_k)));
+
+    // Lambert term (frag:107-110); a zero (or NaN) normal gives 0
+    const float n2 = __fadd_rn(__fadd_rn(__fmul_rn(n[0], n[0]), __fmul_rn(n[1], n[1])), __fmul_rn(n[2], n[2]));
+    float di = 0.0f;
+    if (n2 > 0.0f) {
+        const float inv = __fdiv_rn(1.0f, __fsqrt_rn(n2));
+        const float d = __fadd_rn(__fadd_rn(__fmul_rn(__fmul_rn(n[0], inv), f.light_dir[0]),
+                                            __fmul_rn(__fmul_rn(n[1], inv), f.light_dir[1])),
+                                  __fmul_rn(__fmul_rn(n[2], inv), f.light_dir[2]));
+        di = fmaxf(d, 0.0f);
+    }
+    const float light = __fadd_rn(f.ambient, __fmul_rn(f.diffuse, di));
+    // front-to-back compositing (frag:112-115):
+    // acc.c += (1 - acc.a) * (c * light * alpha), acc.a += (1 - acc.a) * alpha
+    const float2 tr = dup2(__fadd_rn(1.0f, -acc_ba.y));
+    const float2 src_rg = __fmul2_rn(__fmul2_rn(crg, dup2(light)), dup2(alpha));
+    const float src_b = __fmul_rn(__fmul_rn(cba.x, light), alpha);
+    const float2 add_rg = __fmul2_rn(tr, src_rg);
+    const float2 add_ba = __fmul2_rn(tr, make_float2(src_b, alpha));
+    acc_rg = make_float2(__fadd_rn(acc_rg.x, add_rg.x), __fadd_rn(acc_rg.y, add_rg.y));
+    acc_ba = make_float2(__fadd_rn(acc_ba.x, add_ba.x), __fadd_rn(acc_ba.y, add_ba.y));
+}
+
+__device__ __forceinline__ uint32_t blend_rgba8(float2 rg, float2 ba) {
+    // SRC_ALPHA / ONE_MINUS_SRC_ALPHA over a cleared UNORM8 target.
+    const float a = fminf(fmaxf(ba.y, 0.0f), 1.0f);
+    const uint32_t r = (uint32_t)rintf(__fmul_rn(__fmul_rn(fminf(fmaxf(rg.x, 0.0f), 1.0f), a), 255.0f));
+    const uint32_t g = (uint32_t)rintf(__fmul_rn(__fmul_rn(fminf(fmaxf(rg.y, 0.0f), 1.0f), a), 255.0f));
+    const uint32_t b = (uint32_t)rintf(__fmul_rn(__fmul_rn(fminf(fmaxf(ba.x, 0.0f), 1.0f), a), 255.0f));
+    const uint32_t al = (uint32_t)rintf(__fmul_rn(__fmul_rn(a, a), 255.0f));
+    return r | (g << 8) | (b << 16) | (al << 24);
+}
+
+// Is a sample of this brick exactly transparent under the job's LUT?
+template <bool SMEM_LUT>
+__device__ __forceinline__ bool brick_clear(const MarchFrame &f, float2 m, const int *prefix) {
+    if (!(m.x == m.x)) return false;  // NaN in the brick
+    const float d0 = __fmul_rn(m.x, f.value_scale), d1 = __fmul_rn(m.y, f.value_scale);
+    const float dlo = fminf(d0, d1), dhi = fmaxf(d0, d1);
+    if (!(dlo == dlo && dhi == dhi)) return false;
+    const float lmax = (float)(f.lut_size - 1);
+    const int ilo = lut_index(floorf(__fadd_rn(__fmul_rn(dlo, f.flut_size), -0.5f)), lmax, f.lut_size);
+    const int ihi = lut_index(__fadd_rn(floorf(__fadd_rn(__fmul_rn(dhi, f.flut_size), -0.5f)), 1.0f),
+                              lmax, f.lut_size);
+    return prefix_entry<SMEM_LUT>(prefix, ihi + 1) == prefix_entry<SMEM_LUT>(prefix, ilo);
+}
+
+// One pixel's ray of volume.frag.glsl:main (lines 70-122).
+template <int LOG2B, int UNROLL, bool NORMALS, bool SMEM_LUT>
+__device__ __forceinline__ void march_ray(const JobDesc &job, int px, int py, const float4 *lut,
+                                          const int *prefix, float2 &acc_rg, float2 &acc_ba,
+                                          unsigned &n_inbox, unsigned &n_shaded) {
+    constexpr int B = 1 << LOG2B, ROW = brick_apron(LOG2B), SLICE = ROW * ROW;
+    constexpr int RECS = brick_records(LOG2B);
+    const MarchFrame &f = job.f;
+    float pos[3], dstep[3];
+    if (!setup_ray(f, px, py, pos, dstep)) return;
+    // (x, y) lanes packed, z scalar; per lane the reference expressions
+    float2 pxy = make_float2(pos[0], pos[1]);
+    float pz = pos[2];
+    const float2 dxy = make_float2(dstep[0], dstep[1]);
+    const float dz = dstep[2];
+    const float2 nbmin_xy = make_float2(-f.bmin[0], -f.bmin[1]);
+    const float2 inv_xy = make_float2(f.inv_ext[0], f.inv_ext[1]);
+    const float2 fext_xy = make_float2(f.fext[0], f.fext[1]);
+    const float nbmin_z = -f.bmin[2], inv_z = f.inv_ext[2], fext_z = f.fext[2];
+    const int nb1 = f.nb[1], nb2 = f.nb[2];
+    bool entered = false;
+    int cur_brick = -1;
+    bool clear = false;
+    const float4 *bp = job.records;
+    int i = 0;
+    for (;;) {
+#pragma unroll
+        for (int u = 0; u < UNROLL; ++u) {
+            if (!(i < f.max_steps && acc_ba.y < 0.99f)) return;
+            // world_to_texture_coords (frag:25-27, 88)
+            const float2 txy = __fmul2_rn(__fadd2_rn(pxy, nbmin_xy), inv_xy);
+            const float tz = __fmul_rn(__fadd_rn(pz, nbmin_z), inv_z);
+            const bool valid = txy.x >= 0.0f && txy.x <= 1.0f && txy.y >= 0.0f &&
+                               txy.y <= 1.0f && tz >= 0.0f && tz <= 1.0f;
+            if (valid) {
+                entered = true;
+                ++n_inbox;
+                // texel coordinate u = t*size - 0.5, lower texel k = floor(u)
+                const float2 sxy = __fmul2_rn(txy, fext_xy);
+                const float ux = __fadd_rn(sxy.x, -0.5f), uy = __fadd_rn(sxy.y, -0.5f);
+                const float uz = __fadd_rn(__fmul_rn(tz, fext_z), -0.5f);
+                const float flx = floorf(ux), fly = floorf(uy), flz = floorf(uz);
+                const int kx = (int)flx + 1, ky = (int)fly + 1, kz = (int)flz + 1;
+                const int id = ((kx >> LOG2B) * nb1 + (ky >> LOG2B)) * nb2 + (kz >> LOG2B);
+                if (id != cur_brick) {
+                    cur_brick = id;
+                    bp = job.records + (size_t)__ldg(job.table + id) * RECS;
+                    clear = job.skip && brick_clear<SMEM_LUT>(f, __ldg(job.minmax + id), prefix);
+                }
+                if (!clear) {
+                    ++n_shaded;
+                    const int j = (kx & (B - 1)) * SLICE + (ky & (B - 1)) * ROW + (kz & (B - 1));
+                    shade_sample<LOG2B, NORMALS, SMEM_LUT>(f, bp + j, __fadd_rn(ux, -flx),
+                                                           __fadd_rn(uy, -fly), __fadd_rn(uz, -flz),
+                                                           lut, acc_rg, acc_ba);
+                }
+            } else {
+                const bool never = entered || (txy.x < 0.0f && dxy.x <= 0.0f) ||
+                                   (txy.x > 1.0f && dxy.x >= 0.0f) ||
+                                   (txy.y < 0.0f && dxy.y <= 0.0f) ||
+                                   (txy.y > 1.0f && dxy.y >= 0.0f) || (tz < 0.0f && dz <= 0.0f) ||
+                                   (tz > 1.0f && dz >= 0.0f);
+                if (never) return;
+            }
+            // current_world_pos += ray_dir * step_size (frag:118)
+            pxy = __fadd2_rn(pxy, dxy);
+            pz = __fadd_rn(pz, dz);
+            ++i;
+        }
+    }
+}
+
+template <int LOG2B, int UNROLL, bool NORMALS, bool SMEM_LUT>
+__device__ __forceinline__ void march_tile(const JobDesc &job, int px, int py, const float4 *lut,
+                                           const int *prefix, int lane) {
+    const bool in_image = px < job.f.width && py < job.f.height;
+    float2 acc_rg = make_float2(0.0f, 0.0f), acc_ba = make_float2(0.0f, 0.0f);
+    unsigned n_inbox = 0, n_shaded = 0;
+    if (in_image)
+        march_ray<LOG2B, UNROLL, NORMALS, SMEM_LUT>(job, px, py, lut, prefix, acc_rg, acc_ba, n_inbox,
+                                                    n_shaded);
+    if (in_image) {
+        const long long idx = (long long)py * job.f.width + px;
+        if (job.out8) job.out8[idx] = blend_rgba8(acc_rg, acc_ba);
+        if (job.outf) job.outf[idx] = make_float4(acc_rg.x, acc_rg.y, acc_ba.x, acc_ba.y);
+    }
+    if (job.counters) {
+        unsigned long long a = n_inbox, b = n_shaded;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_xor_sync(0xffffffffu, a, o);
+            b += __shfl_xor_sync(0xffffffffu, b, o);
+        }
+        if (lane == 0 && a) {
+            atomicAdd(job.counters, a);
+            atomicAdd(job.counters + 1, b);
+        }
+    }
+}
+
+// Persistent batch kernel.  Dynamic shared memory: lut_smem_entries float4
+// LUT entries followed by lut_smem_entries + 1 prefix counts.
+template <int LOG2B, int UNROLL>
+__global__ void __launch_bounds__(kBatchThreads, 4)
+march_batch_kernel(const BatchHeader *__restrict__ hdr, const int *__restrict__ tile_bases,
+                   const JobDesc *__restrict__ jobs, int *__restrict__ work, int lut_smem_entries) {
+    extern __shared__ float4 s_dyn[];
+    float4 *s_lut = s_dyn;
+    int *s_prefix = reinterpret_cast<int *>(s_dyn + lut_smem_entries);
+    __shared__ JobDesc s_job;
+    __shared__ int s_tile, s_job_idx;
+    const int njobs = hdr->njobs, total = hdr->total_tiles;
+    const int tile_w = hdr->tile_w, tile_h = hdr->tile_h;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int warps_x = tile_w >> 3;
+    const int sub_x = (warp % warps_x) * 8 + (lane & 7);
+    const int sub_y = (warp / warps_x) * 4 + (lane >> 3);
+    int cur_job = -1;
+    bool lut_in_smem = false;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const int t = atomicAdd(work, 1);
+            int lo = 0, hi = njobs - 1;  // last job whose first tile is <= t
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (tile_bases[mid] <= t) lo = mid; else hi = mid - 1;
+            }
+            s_tile = t;
+            s_job_idx = lo;
+        }
+        __syncthreads();
+        const int t = s_tile, j = s_job_idx;
+        if (t >= total) break;
+        if (j != cur_job) {
+            // cache the job descriptor and stage its LUT
+            const int *src = reinterpret_cast<const int *>(jobs + j);
+            int *dst = reinterpret_cast<int *>(&s_job);
+            for (int w = threadIdx.x; w < (int)(sizeof(JobDesc) / 4); w += kBatchThreads) dst[w] = src[w];
+            __syncthreads();
+            lut_in_smem = s_job.f.lut_size <= lut_smem_entries;
+            if (lut_in_smem) {
+                for (int k = threadIdx.x; k < s_job.f.lut_size; k += kBatchThreads) s_lut[k] = s_job.lut[k];
+                for (int k = threadIdx.x; k <= s_job.f.lut_size; k += kBatchThreads) s_prefix[k] = s_job.prefix[k];
+            }
+            __syncthreads();
+            cur_job = j;
+        }
+        const int local = t - s_job.tile_base;
+        const int px = (local % s_job.tiles_x) * tile_w + sub_x;
+        const int py = (local / s_job.tiles_x) * tile_h + sub_y;
+        if (s_job.normals) {
+            if (lut_in_smem) march_tile<LOG2B, UNROLL, true, true>(s_job, px, py, s_lut, s_prefix, lane);
+            else march_tile<LOG2B, UNROLL, true, false>(s_job, px, py, s_job.lut, s_job.prefix, lane);
+        } else {
+            if (lut_in_smem) march_tile<LOG2B, UNROLL, false, true>(s_job, px, py, s_lut, s_prefix, lane);
+            else march_tile<LOG2B, UNROLL, false, false>(s_job, px, py, s_job.lut, s_job.prefix, lane);
+        }
+        __syncthreads();  // s_tile / s_job are rewritten next round
+    }
+}
+
+template <int LOG2B>
+cudaError_t launch_batch_log2(const Tuning &t, const BatchHeader *hdr, const int *tile_bases,
+                              const JobDesc *jobs, int *work, int grid, int lut_smem_entries,
+                              cudaStream_t st) {
+    const size_t shm = (size_t)lut_smem_entries * sizeof(float4) + (size_t)(lut_smem_entries + 1) * sizeof(int);
+    if (t.steps_per_iter >= 4)
+        march_batch_kernel<LOG2B, 4><<<grid, kBatchThreads, shm, st>>>(hdr, tile_bases, jobs, work, lut_smem_entries);
+    else
+        march_batch_kernel<LOG2B, 1><<<grid, kBatchThreads, shm, st>>>(hdr, tile_bases, jobs, work, lut_smem_entries);
+    return cudaGetLastError();
+}
+
+template <int LOG2B>
+int max_blocks_log2(const Tuning &t, int lut_smem_entries) {
+    const size_t shm = (size_t)lut_smem_entries * sizeof(float4) + (size_t)(lut_smem_entries + 1) * sizeof(int);
+    int n = 0;
+    if (t.steps_per_iter >= 4)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, march_batch_kernel<LOG2B, 4>, kBatchThreads, shm);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, march_batch_kernel<LOG2B, 1>, kBatchThreads, shm);
+    return n;
+}
+
+}  // namespace pvr

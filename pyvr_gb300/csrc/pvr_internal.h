@@ -4,50 +4,129 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
 #include <vector>
 
 #include "../../include/pyvr_gb300.h"
+#include "pvr_device.cuh"
 
 namespace pvr {
 
-struct MarchFrame;
+// Brick of (2^log2)^3 texels, stored as (2^log2 + 1)^3 16-byte records
+// (see layout.cu).  Supported sizes: 4, 8, 16.
+constexpr int kMinBrickLog2 = 2;
+constexpr int kMaxBrickLog2 = 4;
+constexpr int kDefaultBrickLog2 = 3;
 
-// A LUT of up to this many RGBA entries is staged in shared memory
-// (48 KiB, the default dynamic shared-memory limit); larger ones are read
-// through the read-only cache.
-constexpr int kLutSmemMaxEntries = 3072;
-
-// Bricks of kBrick^3 texels, stored with a one-texel apron on the high side
-// of each axis: (kBrick+1)^3 16-byte records per brick.
-constexpr int kBrickLog2 = 3;
-constexpr int kBrick = 1 << kBrickLog2;
-constexpr int kApron = kBrick + 1;
-constexpr int kRecordsPerBrick = kApron * kApron * kApron;
-constexpr uint32_t kSlotMask = 0x7fffffffu;
-constexpr uint32_t kTransparentBit = 0x80000000u;
+__host__ __device__ constexpr int brick_apron(int log2b) { return (1 << log2b) + 1; }
+__host__ __device__ constexpr int brick_records(int log2b) {
+    return brick_apron(log2b) * brick_apron(log2b) * brick_apron(log2b);
+}
 
 // Brick grid of one volume; axes are world x, y, z (= W, H, D of the
-// (D,H,W) array).
+// (D,H,W) array).  nb = extent / brick + 1 (see layout.cu).
 struct BrickGeometry {
     int ext[3];
     int nb[3];
     int nbricks;
+    int log2b;
 };
 
-BrickGeometry make_brick_geometry(const int dims_dhw[3]);
+BrickGeometry make_brick_geometry(const int dims_dhw[3], int log2b);
 std::vector<uint32_t> morton_slots(const BrickGeometry &g);
 
-cudaError_t launch_build_records(const BrickGeometry &g, int dtype, const void *vol, const float *nrm,
-                                 const uint32_t *table, float4 *records, float2 *minmax,
-                                 cudaStream_t st);
-cudaError_t launch_brick_flags(const BrickGeometry &g, float value_scale, int lut_size,
-                               const int *opaque_prefix, bool enable, const float2 *minmax,
-                               uint32_t *table, cudaStream_t st);
+// normals_mode: 0 none, 1 from `nrm` (float32 (D,H,W,3)), 2 computed on the
+// device from the stored values (numpy.gradient semantics).
+cudaError_t launch_build_records(const BrickGeometry &g, int dtype, const void *vol, const int dims[3],
+                                 const float *nrm, int normals_mode, const uint32_t *table,
+                                 float4 *records, float2 *minmax, cudaStream_t st);
+cudaError_t launch_read_normals(const BrickGeometry &g, const int dims[3], const uint32_t *table,
+                                const float4 *records, float *out, cudaStream_t st);
 
-// counters[0] = in-box samples (reference loop iterations with a valid
-// texture coordinate), counters[1] = samples actually shaded (not skipped).
-cudaError_t launch_march(const MarchFrame &f, const float4 *records, const uint32_t *table,
-                         bool normals, const float4 *lut, uint32_t *out8, float4 *outf,
-                         unsigned long long *counters, cudaStream_t st);
+// One render of a batch, as the march kernel reads it.
+struct JobDesc {
+    MarchFrame f;
+    const float4 *records;
+    const uint32_t *table;
+    const float2 *minmax;
+    const float4 *lut;
+    const int *prefix;  // prefix[i] = LUT entries before i that are not exactly clear
+    uint32_t *out8;
+    float4 *outf;
+    unsigned long long *counters;  // [in-box samples, shaded samples] or null
+    int tiles_x, tiles_y, tile_base;
+    int normals;
+    int skip;  // empty-space skipping allowed (finite light terms)
+    int pad_[3];
+};
+
+struct BatchHeader {
+    int njobs;
+    int total_tiles;
+    int tile_w, tile_h;
+};
+
+constexpr int kBatchThreads = 256;
+
+// Launch tuning.  tile_w * tile_h == 256 with tile_w a multiple of 8 and
+// tile_h a multiple of 4 (8x4-pixel warp tiles); steps_per_iter in {1, 4};
+// blocks_per_sm: persistent blocks per SM.
+struct Tuning {
+    int tile_w = 16, tile_h = 16;
+    int steps_per_iter = 1;
+    int blocks_per_sm = 4;
+};
+
+// Persistent batch march (march_core.cuh), one instantiation per brick size.
+cudaError_t launch_march_batch(int log2b, const Tuning &t, const BatchHeader *hdr,
+                               const int *tile_bases, const JobDesc *jobs, int *work, int grid,
+                               int lut_smem_entries, cudaStream_t st);
+int max_batch_blocks_per_sm(int log2b, const Tuning &t, int lut_smem_entries);
 
 }  // namespace pvr
+
+// ---------------------------------------------------------------------------
+// C-ABI resource objects (resources.cu)
+// ---------------------------------------------------------------------------
+
+struct pvr_volume {
+    int device = 0;
+    int dtype = PVR_F32;
+    int dims[3] = {0, 0, 0};  // D, H, W
+    float value_scale = 1.0f;
+    float bmin[3] = {-0.5f, -0.5f, -0.5f}, bmax[3] = {0.5f, 0.5f, 0.5f};
+    void *d_vol = nullptr;
+    size_t vol_bytes = 0;
+    float *d_nrm = nullptr;   // given normals, held until the records are built
+    int normals_mode = 0;     // 0 none, 1 given, 2 computed on the device
+    int log2b = pvr::kDefaultBrickLog2;
+    pvr::BrickGeometry geo = {};
+    float4 *d_records = nullptr;
+    size_t records_bytes = 0;
+    uint32_t *d_table = nullptr;
+    float2 *d_minmax = nullptr;
+    bool layout_ready = false;
+};
+
+struct pvr_lut {
+    int device = 0;
+    int size = 0, cap = 0;
+    float4 *d_lut = nullptr;
+    int *d_prefix = nullptr;
+};
+
+namespace pvr {
+// helpers shared by the C-ABI translation units
+int fail(int code, const char *fmt, ...);
+int cuda_fail(cudaError_t e, const char *what);
+int ensure_volume_layout(pvr_volume *v, cudaStream_t st);
+bool invert_gl(const float gl[16], double inv[16]);
+void light_direction(const float pos[3], const float target[3], float out[3]);
+int fill_job(const pvr_job &j, int tile_w, int tile_h, JobDesc &out);
+}  // namespace pvr
+
+#define PVR_CUDA(expr)                                                  \
+    do {                                                                \
+        cudaError_t e_ = (expr);                                        \
+        if (e_ != cudaSuccess) return ::pvr::cuda_fail(e_, #expr);      \
+    } while (0)

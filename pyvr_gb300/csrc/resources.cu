@@ -1,0 +1,334 @@
+// Device resources of the C ABI: volumes (the voxel + normal textures of
+// pyvr/moderngl_renderer/manager.py:77-135 as bricked texel records) and
+// RGBA LUTs (manager.py:137-186), plus the host-side derivations shared by
+// the renderer and the batch launcher.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "pvr_internal.h"
+
+namespace {
+thread_local std::string g_last_error;
+size_t dtype_size(int dtype) { return dtype == PVR_U8 ? 1 : dtype == PVR_F16 ? 2 : 4; }
+bool finite3(const float v[3]) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); }
+}  // namespace
+
+namespace pvr {
+
+int fail(int code, const char *fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+    return fail(e == cudaErrorMemoryAllocation ? PVR_ERR_NOMEM : PVR_ERR_CUDA, "%s: %s", what,
+                cudaGetErrorString(e));
+}
+
+// Inverse of the GL matrix stored column-major in `gl`, in double, by
+// Gauss-Jordan elimination with partial pivoting; inv[r*4+c].
+bool invert_gl(const float gl[16], double inv[16]) {
+    double a[4][8];
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) {
+            a[r][c] = (double)gl[c * 4 + r];
+            a[r][c + 4] = r == c ? 1.0 : 0.0;
+        }
+    for (int col = 0; col < 4; ++col) {
+        int piv = col;
+        for (int r = col + 1; r < 4; ++r)
+            if (std::fabs(a[r][col]) > std::fabs(a[piv][col])) piv = r;
+        if (a[piv][col] == 0.0 || std::isnan(a[piv][col])) return false;
+        if (piv != col)
+            for (int c = 0; c < 8; ++c) std::swap(a[piv][c], a[col][c]);
+        const double p = a[col][col];
+        for (int c = 0; c < 8; ++c) a[col][c] /= p;
+        for (int r = 0; r < 4; ++r) {
+            if (r == col) continue;
+            const double m = a[r][col];
+            if (m == 0.0) continue;
+            for (int c = 0; c < 8; ++c) a[r][c] -= m * a[col][c];
+        }
+    }
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) inv[r * 4 + c] = a[r][c + 4];
+    return true;
+}
+
+// normalize(light_target - light_position) (volume.frag.glsl:107); 0 for a
+// degenerate light, whose diffuse term the shader's max(dot(NaN,L),0) zeroes.
+void light_direction(const float pos[3], const float target[3], float out[3]) {
+    float l[3];
+    for (int a = 0; a < 3; ++a) l[a] = target[a] - pos[a];
+    const float l2 = (l[0] * l[0] + l[1] * l[1]) + l[2] * l[2];
+    const float li = l2 > 0.0f ? 1.0f / std::sqrt(l2) : 0.0f;
+    for (int a = 0; a < 3; ++a) out[a] = l[a] * li;
+}
+
+// Records, brick table and value ranges of a volume (once per volume).
+int ensure_volume_layout(pvr_volume *v, cudaStream_t st) {
+    if (v->layout_ready) return PVR_OK;
+    cudaFree(v->d_records);
+    cudaFree(v->d_table);
+    cudaFree(v->d_minmax);
+    v->d_records = nullptr;
+    v->d_table = nullptr;
+    v->d_minmax = nullptr;
+    v->records_bytes = 0;
+    v->geo = make_brick_geometry(v->dims, v->log2b);
+    std::vector<uint32_t> table = morton_slots(v->geo);
+    const size_t nrec = (size_t)v->geo.nbricks * brick_records(v->log2b);
+    PVR_CUDA(cudaMalloc(&v->d_records, nrec * sizeof(float4)));
+    v->records_bytes = nrec * sizeof(float4);
+    PVR_CUDA(cudaMalloc(&v->d_table, table.size() * sizeof(uint32_t)));
+    PVR_CUDA(cudaMalloc(&v->d_minmax, table.size() * sizeof(float2)));
+    PVR_CUDA(cudaMemcpyAsync(v->d_table, table.data(), table.size() * sizeof(uint32_t),
+                             cudaMemcpyHostToDevice, st));
+    PVR_CUDA(launch_build_records(v->geo, v->dtype, v->d_vol, v->dims, v->d_nrm, v->normals_mode,
+                                  v->d_table, v->d_records, v->d_minmax, st));
+    PVR_CUDA(cudaStreamSynchronize(st));  // `table` leaves scope
+    cudaFree(v->d_nrm);  // given normals now live in the records
+    v->d_nrm = nullptr;
+    v->layout_ready = true;
+    return PVR_OK;
+}
+
+// Validated job -> the descriptor the kernel reads (everything the fragment
+// shader derives per fragment but that is constant over the frame).
+int fill_job(const pvr_job &j, int tile_w, int tile_h, JobDesc &out) {
+    std::memset(&out, 0, sizeof(out));
+    if (!j.volume || !j.lut) return fail(PVR_ERR_VALUE, "job without volume or LUT");
+    if (!j.volume->layout_ready) return fail(PVR_ERR_STATE, "volume layout not built");
+    if (j.width <= 0 || j.height <= 0 || j.width > 32768 || j.height > 32768)
+        return fail(PVR_ERR_VALUE, "job size must be in 1..32768, got %dx%d", j.width, j.height);
+    if (!(j.step_size > 0.0f) || !std::isfinite(j.step_size) || !(j.reference_step_size > 0.0f) ||
+        !std::isfinite(j.reference_step_size) || j.max_steps < 1)
+        return fail(PVR_ERR_VALUE, "invalid step_size / reference_step_size / max_steps");
+    const pvr_volume &v = *j.volume;
+    MarchFrame &f = out.f;
+    double ip[16], iv[16];
+    if (!invert_gl(j.proj, ip)) return fail(PVR_ERR_VALUE, "projection matrix is singular");
+    if (!invert_gl(j.view, iv)) return fail(PVR_ERR_VALUE, "view matrix is singular");
+    for (int i = 0; i < 8; ++i) f.ip[i] = (float)ip[i];
+    for (int i = 0; i < 12; ++i) f.iv[i] = (float)iv[i];
+    f.width = j.width;
+    f.height = j.height;
+    for (int a = 0; a < 3; ++a) {
+        f.cam[a] = j.camera_pos[a];
+        f.bmin[a] = v.bmin[a];
+        f.bmax[a] = v.bmax[a];
+        f.inv_ext[a] = 1.0f / (v.bmax[a] - v.bmin[a]);
+        // world x <-> texture r (extent W), y <-> t (H), z <-> s (D)
+        f.ext[a] = v.geo.ext[a];
+        f.fext[a] = (float)v.geo.ext[a];
+        f.nb[a] = v.geo.nb[a];
+    }
+    f.step = j.step_size;
+    f.alpha_k = j.step_size / j.reference_step_size;
+    f.max_steps = j.max_steps;
+    light_direction(j.light_pos, j.light_target, f.light_dir);
+    f.ambient = j.ambient;
+    f.diffuse = j.diffuse;
+    f.value_scale = v.value_scale;
+    f.lut_size = j.lut->size;
+    f.flut_size = (float)j.lut->size;
+    out.records = v.d_records;
+    out.table = v.d_table;
+    out.minmax = v.d_minmax;
+    out.lut = j.lut->d_lut;
+    out.prefix = j.lut->d_prefix;
+    out.out8 = (uint32_t *)j.d_rgba8;
+    out.outf = (float4 *)j.d_rgba32f;
+    out.counters = j.d_counters;
+    out.tiles_x = (j.width + tile_w - 1) / tile_w;
+    out.tiles_y = (j.height + tile_h - 1) / tile_h;
+    out.normals = v.normals_mode != PVR_NORMALS_NONE;
+    out.skip = std::isfinite(j.ambient) && std::isfinite(j.diffuse);
+    return PVR_OK;
+}
+
+}  // namespace pvr
+
+using pvr::fail;
+
+extern "C" {
+
+int pvr_abi_version(void) { return PVR_ABI_VERSION; }
+
+const char *pvr_last_error(void) { return g_last_error.c_str(); }
+
+int pvr_volume_create(const void *data, int dtype, int d, int h, int w, float value_scale,
+                      const float min_bounds[3], const float max_bounds[3], const float *normals,
+                      int normals_mode, int brick_log2, pvr_volume **out) {
+    if (!out) return fail(PVR_ERR_VALUE, "out is NULL");
+    *out = nullptr;
+    if (!data) return fail(PVR_ERR_VALUE, "volume data is NULL");
+    if (dtype != PVR_U8 && dtype != PVR_F16 && dtype != PVR_F32)
+        return fail(PVR_ERR_TYPE, "unsupported volume dtype code %d", dtype);
+    if (d <= 0 || h <= 0 || w <= 0) return fail(PVR_ERR_VALUE, "Volume data must be 3D with positive extents");
+    if ((long long)d * h * w > (1LL << 31)) return fail(PVR_ERR_VALUE, "volume larger than 2^31 voxels");
+    if (!min_bounds || !max_bounds || !finite3(min_bounds) || !finite3(max_bounds))
+        return fail(PVR_ERR_VALUE, "bounds must be three finite floats each");
+    for (int a = 0; a < 3; ++a)
+        if (!(max_bounds[a] > min_bounds[a])) return fail(PVR_ERR_VALUE, "max_bounds must be greater than min_bounds");
+    if (!std::isfinite(value_scale)) return fail(PVR_ERR_VALUE, "value_scale must be finite");
+    if (normals_mode < PVR_NORMALS_NONE || normals_mode > PVR_NORMALS_DEVICE)
+        return fail(PVR_ERR_VALUE, "unknown normals mode %d", normals_mode);
+    if (normals_mode == PVR_NORMALS_GIVEN && !normals) return fail(PVR_ERR_VALUE, "normals are NULL");
+    if (normals_mode == PVR_NORMALS_DEVICE && (d < 2 || h < 2 || w < 2))
+        return fail(PVR_ERR_VALUE, "Shape of array too small to calculate a numerical gradient, "
+                                   "at least (edge_order + 1) elements are required.");
+    if (brick_log2 == 0) brick_log2 = pvr::kDefaultBrickLog2;
+    if (brick_log2 < pvr::kMinBrickLog2 || brick_log2 > pvr::kMaxBrickLog2)
+        return fail(PVR_ERR_VALUE, "brick_log2 must be 2, 3 or 4");
+    pvr_volume *v = new pvr_volume();
+    cudaGetDevice(&v->device);
+    v->dtype = dtype;
+    v->dims[0] = d;
+    v->dims[1] = h;
+    v->dims[2] = w;
+    v->value_scale = value_scale;
+    v->normals_mode = normals_mode;
+    v->log2b = brick_log2;
+    for (int a = 0; a < 3; ++a) {
+        v->bmin[a] = min_bounds[a];
+        v->bmax[a] = max_bounds[a];
+    }
+    const size_t nvox = (size_t)d * h * w;
+    auto bail = [&](int rc) {
+        cudaFree(v->d_vol);
+        cudaFree(v->d_nrm);
+        cudaFree(v->d_records);
+        cudaFree(v->d_table);
+        cudaFree(v->d_minmax);
+        delete v;
+        return rc;
+    };
+    cudaError_t e = cudaMalloc(&v->d_vol, nvox * dtype_size(dtype));
+    if (e != cudaSuccess) return bail(pvr::cuda_fail(e, "cudaMalloc(volume)"));
+    v->vol_bytes = nvox * dtype_size(dtype);
+    e = cudaMemcpy(v->d_vol, data, v->vol_bytes, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return bail(pvr::cuda_fail(e, "cudaMemcpy(volume)"));
+    if (normals_mode == PVR_NORMALS_GIVEN) {
+        e = cudaMalloc(&v->d_nrm, nvox * 3 * sizeof(float));
+        if (e != cudaSuccess) return bail(pvr::cuda_fail(e, "cudaMalloc(normals)"));
+        e = cudaMemcpy(v->d_nrm, normals, nvox * 3 * sizeof(float), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return bail(pvr::cuda_fail(e, "cudaMemcpy(normals)"));
+    }
+    if (int rc = pvr::ensure_volume_layout(v, 0)) return bail(rc);
+    *out = v;
+    return PVR_OK;
+}
+
+int pvr_volume_destroy(pvr_volume *v) {
+    if (!v) return PVR_OK;
+    cudaDeviceSynchronize();  // no batch may still read it
+    cudaFree(v->d_vol);
+    cudaFree(v->d_nrm);
+    cudaFree(v->d_records);
+    cudaFree(v->d_table);
+    cudaFree(v->d_minmax);
+    delete v;
+    return PVR_OK;
+}
+
+int pvr_volume_device_bytes(const pvr_volume *v, long long *bytes) {
+    if (!v || !bytes) return fail(PVR_ERR_VALUE, "NULL argument");
+    *bytes = (long long)(v->vol_bytes + v->records_bytes +
+                         (size_t)v->geo.nbricks * (sizeof(uint32_t) + sizeof(float2)));
+    return PVR_OK;
+}
+
+int pvr_volume_read_normals(const pvr_volume *v, float *normals_out) {
+    if (!v || !normals_out) return fail(PVR_ERR_VALUE, "NULL argument");
+    if (!v->layout_ready) return fail(PVR_ERR_STATE, "volume layout not built");
+    const size_t n = (size_t)v->dims[0] * v->dims[1] * v->dims[2] * 3;
+    float *d = nullptr;
+    PVR_CUDA(cudaMalloc(&d, n * sizeof(float)));
+    cudaError_t e = pvr::launch_read_normals(v->geo, v->dims, v->d_table, v->d_records, d, 0);
+    if (e == cudaSuccess) e = cudaMemcpy(normals_out, d, n * sizeof(float), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return pvr::cuda_fail(e, "read normals");
+    return PVR_OK;
+}
+
+int pvr_lut_create(const float *rgba, int size, pvr_lut **out) {
+    if (!out) return fail(PVR_ERR_VALUE, "out is NULL");
+    *out = nullptr;
+    pvr_lut *l = new pvr_lut();
+    cudaGetDevice(&l->device);
+    int rc = pvr_lut_update(l, rgba, size);
+    if (rc != PVR_OK) {
+        pvr_lut_destroy(l);
+        return rc;
+    }
+    *out = l;
+    return PVR_OK;
+}
+
+int pvr_lut_update(pvr_lut *l, const float *rgba, int size) {
+    if (!l) return fail(PVR_ERR_VALUE, "null LUT handle");
+    if (!rgba) return fail(PVR_ERR_VALUE, "LUT is NULL");
+    if (size <= 0 || size > (1 << 24)) return fail(PVR_ERR_VALUE, "LUT size must be in 1..2^24, got %d", size);
+    if (size > l->cap) {
+        cudaDeviceSynchronize();  // a queued batch may still read the old table
+        cudaFree(l->d_lut);
+        cudaFree(l->d_prefix);
+        l->d_lut = nullptr;
+        l->d_prefix = nullptr;
+        l->cap = 0;
+        PVR_CUDA(cudaMalloc(&l->d_lut, (size_t)size * sizeof(float4)));
+        PVR_CUDA(cudaMalloc(&l->d_prefix, (size_t)(size + 1) * sizeof(int)));
+        l->cap = size;
+    }
+    // prefix[i] = entries before i that a skipped sample must not read:
+    // alpha not exactly 0, or a non-finite colour
+    std::vector<int> prefix(size + 1, 0);
+    for (int i = 0; i < size; ++i) {
+        const float *e = rgba + 4 * i;
+        const bool clear = e[3] == 0.0f && std::isfinite(e[0]) && std::isfinite(e[1]) && std::isfinite(e[2]);
+        prefix[i + 1] = prefix[i] + (clear ? 0 : 1);
+    }
+    // synchronous copies: ordered after every earlier launch on the legacy stream
+    PVR_CUDA(cudaMemcpy(l->d_lut, rgba, (size_t)size * sizeof(float4), cudaMemcpyHostToDevice));
+    PVR_CUDA(cudaMemcpy(l->d_prefix, prefix.data(), (size_t)(size + 1) * sizeof(int), cudaMemcpyHostToDevice));
+    l->size = size;
+    return PVR_OK;
+}
+
+int pvr_lut_destroy(pvr_lut *l) {
+    if (!l) return PVR_OK;
+    cudaDeviceSynchronize();
+    cudaFree(l->d_lut);
+    cudaFree(l->d_prefix);
+    delete l;
+    return PVR_OK;
+}
+
+int pvr_frame_constants(const float view[16], const float proj[16], const float light_pos[3],
+                        const float light_target[3], const float min_bounds[3],
+                        const float max_bounds[3], float step_size, float reference_step_size,
+                        float out[27]) {
+    if (!view || !proj || !light_pos || !light_target || !min_bounds || !max_bounds || !out)
+        return fail(PVR_ERR_VALUE, "NULL argument");
+    double ip[16], iv[16];
+    if (!pvr::invert_gl(proj, ip)) return fail(PVR_ERR_VALUE, "projection matrix is singular");
+    if (!pvr::invert_gl(view, iv)) return fail(PVR_ERR_VALUE, "view matrix is singular");
+    for (int i = 0; i < 8; ++i) out[i] = (float)ip[i];
+    for (int i = 0; i < 12; ++i) out[8 + i] = (float)iv[i];
+    pvr::light_direction(light_pos, light_target, out + 20);
+    for (int a = 0; a < 3; ++a) out[23 + a] = 1.0f / (max_bounds[a] - min_bounds[a]);
+    out[26] = step_size / reference_step_size;
+    return PVR_OK;
+}
+
+}  // extern "C"

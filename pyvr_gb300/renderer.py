@@ -208,6 +208,17 @@ class CudaVolumeRenderer:
         image = Image.frombytes("RGBA", (self.width, self.height), data)
         return image.transpose(Image.FLIP_TOP_BOTTOM)
 
+    def compute_normals(self) -> None:
+        """Volume.compute_normals on the GPU for the loaded volume (the
+        normals numpy's compute_normal_volume would give, bit for bit)."""
+        check(self._lib.pvr_compute_normals(self._handle()))
+
+    def set_tuning(self, tile_w: int = 16, tile_h: int = 16, steps_per_iter: int = 1,
+                   blocks_per_sm: int = 0) -> None:
+        """Launch shape of the march (any valid shape gives the same image)."""
+        t = _native.PvrTuning(tile_w, tile_h, steps_per_iter, blocks_per_sm)
+        check(self._lib.pvr_set_tuning(self._handle(), ctypes.byref(t)))
+
     def last_sample_count(self) -> int:
         n = ctypes.c_longlong(0)
         check(self._lib.pvr_last_sample_count(self._handle(), ctypes.byref(n)))
