@@ -1,38 +1,50 @@
 // Batched rendering: many renders in one persistent kernel launch.
 //
-// A launcher owns `slots` staging areas.  Each slot is a pinned host block
-// and a device block holding {BatchHeader, tile bases, JobDesc[capacity]},
-// a work counter, and a CUDA graph captured once per launch configuration:
-// [copy host block -> device block, zero the work counter, persistent march
-// kernel].  Queuing a batch fills the next slot's pinned block and launches
-// its graph; a slot is reused only after the event recorded behind its last
-// graph launch has completed, so up to `slots` batches can be in flight.
+// A launcher owns `slots` launch slots.  Each slot has its own work counter
+// and a CUDA graph [zero the counter -> persistent march kernel] built once
+// per launch configuration (brick size, tuning, grid, LUT staging size).
+// Queuing a batch writes the job table into the kernel node's parameters
+// (cudaGraphExecKernelNodeSetParams) and launches the slot's graph; a slot
+// is reused only after the event recorded behind its last launch has
+// completed, so up to `slots` batches can be in flight.  Batches of more
+// than kMaxLaunchJobs jobs are split over consecutive launches.
 #include <algorithm>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <vector>
 
 #include "pvr_internal.h"
 
 namespace pvr {
-cudaError_t launch_march_batch_b2(const Tuning &, const BatchHeader *, const int *, const JobDesc *, int *,
-                                  int, int, cudaStream_t);
-cudaError_t launch_march_batch_b3(const Tuning &, const BatchHeader *, const int *, const JobDesc *, int *,
-                                  int, int, cudaStream_t);
-cudaError_t launch_march_batch_b4(const Tuning &, const BatchHeader *, const int *, const JobDesc *, int *,
-                                  int, int, cudaStream_t);
+const void *batch_kernel_b2(const Tuning &);
+const void *batch_kernel_b3(const Tuning &);
+const void *batch_kernel_b4(const Tuning &);
+const void *single_kernel_b2(const Tuning &);
+const void *single_kernel_b3(const Tuning &);
+const void *single_kernel_b4(const Tuning &);
 int max_batch_blocks_b2(const Tuning &, int);
 int max_batch_blocks_b3(const Tuning &, int);
 int max_batch_blocks_b4(const Tuning &, int);
 
-cudaError_t launch_march_batch(int log2b, const Tuning &t, const BatchHeader *hdr, const int *tile_bases,
-                               const JobDesc *jobs, int *work, int grid, int lut_smem_entries,
-                               cudaStream_t st) {
+const void *batch_kernel(int log2b, const Tuning &t) {
     switch (log2b) {
-    case 2: return launch_march_batch_b2(t, hdr, tile_bases, jobs, work, grid, lut_smem_entries, st);
-    case 4: return launch_march_batch_b4(t, hdr, tile_bases, jobs, work, grid, lut_smem_entries, st);
-    default: return launch_march_batch_b3(t, hdr, tile_bases, jobs, work, grid, lut_smem_entries, st);
+    case 2: return batch_kernel_b2(t);
+    case 4: return batch_kernel_b4(t);
+    default: return batch_kernel_b3(t);
     }
+}
+
+const void *single_kernel(int log2b, const Tuning &t) {
+    switch (log2b) {
+    case 2: return single_kernel_b2(t);
+    case 4: return single_kernel_b4(t);
+    default: return single_kernel_b3(t);
+    }
+}
+
+size_t batch_smem_bytes(int lut_smem_entries) {
+    return (size_t)lut_smem_entries * sizeof(float4) + (size_t)(lut_smem_entries + 1) * sizeof(int);
 }
 
 int max_batch_blocks_per_sm(int log2b, const Tuning &t, int lut_smem_entries) {
@@ -47,24 +59,20 @@ int max_batch_blocks_per_sm(int log2b, const Tuning &t, int lut_smem_entries) {
 namespace {
 
 struct LaunchKey {
-    int log2b = -1, tile_w = 0, tile_h = 0, steps = 0, grid = 0, lut_smem = 0;
-    bool operator==(const LaunchKey &o) const {
-        return log2b == o.log2b && tile_w == o.tile_w && tile_h == o.tile_h && steps == o.steps &&
-               grid == o.grid && lut_smem == o.lut_smem;
-    }
+    const void *fn = nullptr;
+    int grid = 0, lut_smem = 0;
+    bool operator==(const LaunchKey &o) const { return fn == o.fn && grid == o.grid && lut_smem == o.lut_smem; }
 };
 
 struct Slot {
-    void *h_block = nullptr;  // pinned
-    void *d_block = nullptr;
     int *d_work = nullptr;
     cudaEvent_t done = nullptr;
     bool pending = false;
+    cudaGraph_t graph = nullptr;  // kept: its kernel node is updated per batch
     cudaGraphExec_t exec = nullptr;
+    cudaGraphNode_t kernel_node = nullptr;
     LaunchKey key;
 };
-
-size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 
 }  // namespace
 
@@ -76,22 +84,21 @@ struct pvr_batch {
     cudaStream_t stream = nullptr;
     pvr::Tuning tuning;
     std::vector<Slot> slots;
-    size_t off_bases = 0, off_jobs = 0, block_bytes = 0;
+    std::unique_ptr<pvr::BatchParams> params;  // host staging of one launch's job table
+    pvr::SingleParams single;                  // ... of a one-job launch
 };
 
 using pvr::fail;
 
 namespace {
 
-int destroy_slot(Slot &s) {
+void destroy_slot(Slot &s) {
     if (s.done) cudaEventSynchronize(s.done);
     if (s.exec) cudaGraphExecDestroy(s.exec);
+    if (s.graph) cudaGraphDestroy(s.graph);
     if (s.done) cudaEventDestroy(s.done);
-    cudaFreeHost(s.h_block);
-    cudaFree(s.d_block);
     cudaFree(s.d_work);
     s = Slot();
-    return PVR_OK;
 }
 
 bool valid_tuning(const pvr::Tuning &t) {
@@ -100,34 +107,125 @@ bool valid_tuning(const pvr::Tuning &t) {
            t.blocks_per_sm >= 0 && t.blocks_per_sm <= 16;
 }
 
-int capture(pvr_batch *b, Slot &s, const LaunchKey &key) {
-    if (s.exec) {
-        cudaGraphExecDestroy(s.exec);
-        s.exec = nullptr;
-    }
-    const auto *hdr = (const pvr::BatchHeader *)s.d_block;
-    const auto *bases = (const int *)((const char *)s.d_block + b->off_bases);
-    const auto *jobs = (const pvr::JobDesc *)((const char *)s.d_block + b->off_jobs);
-    pvr::Tuning t = b->tuning;
-    PVR_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-    cudaError_t e = cudaMemcpyAsync(s.d_block, s.h_block, b->block_bytes, cudaMemcpyHostToDevice, b->stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(s.d_work, 0, sizeof(int), b->stream);
-    if (e == cudaSuccess)
-        e = pvr::launch_march_batch(key.log2b, t, hdr, bases, jobs, s.d_work, key.grid, key.lut_smem, b->stream);
-    cudaGraph_t graph = nullptr;
-    cudaError_t e2 = cudaStreamEndCapture(b->stream, &graph);
+cudaKernelNodeParams kernel_params(const LaunchKey &key, void **args) {
+    cudaKernelNodeParams kp;
+    std::memset(&kp, 0, sizeof(kp));
+    kp.func = const_cast<void *>(key.fn);
+    kp.gridDim = dim3(key.grid);
+    kp.blockDim = dim3(pvr::kBatchThreads);
+    kp.sharedMemBytes = (unsigned)pvr::batch_smem_bytes(key.lut_smem);
+    kp.kernelParams = args;
+    kp.extra = nullptr;
+    return kp;
+}
+
+// [memset(work) -> kernel] for this slot and launch configuration
+int build_graph(Slot &s, const LaunchKey &key, void **args) {
+    if (s.exec) cudaGraphExecDestroy(s.exec);
+    if (s.graph) cudaGraphDestroy(s.graph);
+    s.exec = nullptr;
+    s.graph = nullptr;
+    s.kernel_node = nullptr;
+    cudaGraph_t g = nullptr;
+    PVR_CUDA(cudaGraphCreate(&g, 0));
+    cudaMemsetParams mp;
+    std::memset(&mp, 0, sizeof(mp));
+    mp.dst = s.d_work;
+    mp.value = 0;
+    mp.elementSize = sizeof(int);
+    mp.width = 1;
+    mp.height = 1;
+    cudaGraphNode_t mset = nullptr;
+    cudaError_t e = cudaGraphAddMemsetNode(&mset, g, nullptr, 0, &mp);
+    cudaKernelNodeParams kp = kernel_params(key, args);
+    if (e == cudaSuccess) e = cudaGraphAddKernelNode(&s.kernel_node, g, &mset, 1, &kp);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&s.exec, g, 0);
     if (e != cudaSuccess) {
-        if (graph) cudaGraphDestroy(graph);
-        return pvr::cuda_fail(e, "batch capture");
-    }
-    if (e2 != cudaSuccess) return pvr::cuda_fail(e2, "cudaStreamEndCapture");
-    e = cudaGraphInstantiate(&s.exec, graph, 0);
-    cudaGraphDestroy(graph);
-    if (e != cudaSuccess) {
+        cudaGraphDestroy(g);
         s.exec = nullptr;
-        return pvr::cuda_fail(e, "cudaGraphInstantiate");
+        s.kernel_node = nullptr;
+        return pvr::cuda_fail(e, "batch graph");
     }
+    s.graph = g;
     s.key = key;
+    return PVR_OK;
+}
+
+int launch_chunk(pvr_batch *b, const pvr_job *jobs, int n, cudaStream_t st) {
+    const int log2b = jobs[0].volume->log2b;
+    int max_lut = 1;
+    for (int i = 0; i < n; ++i) max_lut = std::max(max_lut, jobs[i].lut->size);
+    Slot &s = b->slots[b->next];
+    if (s.pending) {
+        PVR_CUDA(cudaEventSynchronize(s.done));
+        s.pending = false;
+    }
+    if (n == 1) {  // one job: the single-job kernel, one block per tile
+        pvr::SingleParams &sp = b->single;
+        if (int rc = pvr::fill_job(jobs[0], b->tuning.tile_w, b->tuning.tile_h, sp.job)) return rc;
+        sp.tile_w = b->tuning.tile_w;
+        sp.tile_h = b->tuning.tile_h;
+        int lut_smem = 256;
+        while (lut_smem < max_lut && lut_smem < 2048) lut_smem *= 2;
+        sp.lut_smem_entries = lut_smem;
+        const long long tiles = (long long)sp.job.tiles_x * sp.job.tiles_y;
+        LaunchKey key;
+        key.fn = pvr::single_kernel(log2b, b->tuning);
+        key.grid = (int)tiles;
+        key.lut_smem = lut_smem;
+        void *args[] = {&sp};
+        if (!s.exec || !(s.key == key)) {
+            if (int rc = build_graph(s, key, args)) return rc;
+        } else {
+            cudaKernelNodeParams kp = kernel_params(key, args);
+            PVR_CUDA(cudaGraphExecKernelNodeSetParams(s.exec, s.kernel_node, &kp));
+        }
+        PVR_CUDA(cudaGraphLaunch(s.exec, st));
+        PVR_CUDA(cudaEventRecord(s.done, st));
+        s.pending = true;
+        b->next = (b->next + 1) % (int)b->slots.size();
+        return PVR_OK;
+    }
+    pvr::BatchParams &p = *b->params;
+    long long total = 0;
+    for (int i = 0; i < n; ++i) {
+        if (int rc = pvr::fill_job(jobs[i], b->tuning.tile_w, b->tuning.tile_h, p.jobs[i])) {
+            const std::string why = pvr_last_error();
+            return fail(rc, "job %d: %s", i, why.c_str());
+        }
+        p.jobs[i].tile_base = (int)total;
+        p.tile_base[i] = (int)total;
+        total += (long long)p.jobs[i].tiles_x * p.jobs[i].tiles_y;
+        if (total > (1LL << 30)) return fail(PVR_ERR_VALUE, "batch has too many tiles");
+    }
+    p.njobs = n;
+    p.total_tiles = (int)total;
+    p.tile_w = b->tuning.tile_w;
+    p.tile_h = b->tuning.tile_h;
+    // LUT staging sized by the largest table (a few fixed sizes so graphs are
+    // reused); larger tables are read through the read-only cache
+    int lut_smem = 256;
+    while (lut_smem < max_lut && lut_smem < 2048) lut_smem *= 2;
+    p.lut_smem_entries = lut_smem;
+    p.work = s.d_work;
+    int per_sm = b->tuning.blocks_per_sm;
+    const int fit = pvr::max_batch_blocks_per_sm(log2b, b->tuning, lut_smem);
+    if (per_sm <= 0 || per_sm > fit) per_sm = std::max(1, fit);
+    LaunchKey key;
+    key.fn = pvr::batch_kernel(log2b, b->tuning);
+    key.grid = b->sms * per_sm;
+    key.lut_smem = lut_smem;
+    void *args[] = {&p};
+    if (!s.exec || !(s.key == key)) {
+        if (int rc = build_graph(s, key, args)) return rc;
+    } else {
+        cudaKernelNodeParams kp = kernel_params(key, args);
+        PVR_CUDA(cudaGraphExecKernelNodeSetParams(s.exec, s.kernel_node, &kp));
+    }
+    PVR_CUDA(cudaGraphLaunch(s.exec, st));
+    PVR_CUDA(cudaEventRecord(s.done, st));
+    s.pending = true;
+    b->next = (b->next + 1) % (int)b->slots.size();
     return PVR_OK;
 }
 
@@ -144,17 +242,13 @@ int pvr_batch_create(int capacity_jobs, int slots, pvr_batch **out) {
     cudaGetDevice(&b->device);
     cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device);
     b->cap = capacity_jobs;
-    b->off_bases = align16(sizeof(pvr::BatchHeader));
-    b->off_jobs = align16(b->off_bases + sizeof(int) * capacity_jobs);
-    b->block_bytes = b->off_jobs + sizeof(pvr::JobDesc) * capacity_jobs;
+    b->params.reset(new pvr::BatchParams());
+    std::memset(b->params.get(), 0, sizeof(pvr::BatchParams));
     b->slots.resize(slots);
     cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
     for (auto &s : b->slots) {
-        if (e == cudaSuccess) e = cudaMallocHost(&s.h_block, b->block_bytes);
-        if (e == cudaSuccess) e = cudaMalloc(&s.d_block, b->block_bytes);
         if (e == cudaSuccess) e = cudaMalloc(&s.d_work, sizeof(int));
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming);
-        if (e == cudaSuccess) std::memset(s.h_block, 0, b->block_bytes);
     }
     if (e != cudaSuccess) {
         int rc = pvr::cuda_fail(e, "pvr_batch_create");
@@ -202,59 +296,14 @@ int pvr_batch_render(pvr_batch *b, const pvr_job *jobs, int n, void *stream) {
     if (n > 0 && !jobs) return fail(PVR_ERR_VALUE, "jobs is NULL");
     if (n == 0) return PVR_OK;
     const int log2b = jobs[0].volume ? jobs[0].volume->log2b : pvr::kDefaultBrickLog2;
-    int max_lut = 1;
     for (int i = 0; i < n; ++i) {
         if (!jobs[i].volume || !jobs[i].lut) return fail(PVR_ERR_VALUE, "job %d without volume or LUT", i);
         if (jobs[i].volume->log2b != log2b)
             return fail(PVR_ERR_VALUE, "all volumes of a batch must share one brick size");
-        max_lut = std::max(max_lut, jobs[i].lut->size);
-    }
-    Slot &s = b->slots[b->next];
-    if (s.pending) {
-        PVR_CUDA(cudaEventSynchronize(s.done));
-        s.pending = false;
-    }
-    // fill the pinned block
-    auto *hdr = (pvr::BatchHeader *)s.h_block;
-    int *bases = (int *)((char *)s.h_block + b->off_bases);
-    auto *descs = (pvr::JobDesc *)((char *)s.h_block + b->off_jobs);
-    long long total = 0;
-    for (int i = 0; i < n; ++i) {
-        if (int rc = pvr::fill_job(jobs[i], b->tuning.tile_w, b->tuning.tile_h, descs[i])) {
-            const std::string why = pvr_last_error();
-            return fail(rc, "job %d: %s", i, why.c_str());
-        }
-        descs[i].tile_base = (int)total;
-        bases[i] = (int)total;
-        total += (long long)descs[i].tiles_x * descs[i].tiles_y;
-        if (total > (1LL << 30)) return fail(PVR_ERR_VALUE, "batch has too many tiles");
-    }
-    hdr->njobs = n;
-    hdr->total_tiles = (int)total;
-    hdr->tile_w = b->tuning.tile_w;
-    hdr->tile_h = b->tuning.tile_h;
-    // launch configuration: LUT staging sized by the largest table (a few
-    // fixed sizes so graphs are reused), persistent grid
-    int lut_smem = 256;
-    while (lut_smem < max_lut && lut_smem < 2048) lut_smem *= 2;
-    int per_sm = b->tuning.blocks_per_sm;
-    const int fit = pvr::max_batch_blocks_per_sm(log2b, b->tuning, lut_smem);
-    if (per_sm <= 0 || per_sm > fit) per_sm = std::max(1, fit);
-    LaunchKey key;
-    key.log2b = log2b;
-    key.tile_w = b->tuning.tile_w;
-    key.tile_h = b->tuning.tile_h;
-    key.steps = b->tuning.steps_per_iter;
-    key.grid = b->sms * per_sm;
-    key.lut_smem = lut_smem;
-    if (!s.exec || !(s.key == key)) {
-        if (int rc = capture(b, s, key)) return rc;
     }
     cudaStream_t st = stream ? (cudaStream_t)stream : b->stream;
-    PVR_CUDA(cudaGraphLaunch(s.exec, st));
-    PVR_CUDA(cudaEventRecord(s.done, st));
-    s.pending = true;
-    b->next = (b->next + 1) % (int)b->slots.size();
+    for (int i0 = 0; i0 < n; i0 += pvr::kMaxLaunchJobs)
+        if (int rc = launch_chunk(b, jobs + i0, std::min(pvr::kMaxLaunchJobs, n - i0), st)) return rc;
     return PVR_OK;
 }
 

@@ -167,16 +167,17 @@ __global__ void build_records_kernel(BrickGeometry g, const T *__restrict__ vol,
 }
 
 // One warp per brick: min/max of the stored values over all its records
-// (the footprints of every sample that maps to it).  A NaN marks the brick
-// as never skippable.
+// (the footprints of every sample that maps to it), stored with the brick's
+// record slot.  A NaN marks the brick as never skippable.
 template <int LOG2B>
 __global__ void brick_minmax_kernel(BrickGeometry g, const uint32_t *__restrict__ table,
-                                    const float4 *__restrict__ records, float2 *__restrict__ mm) {
+                                    const float4 *__restrict__ records, uint4 *__restrict__ bricks) {
     constexpr int R = brick_records(LOG2B);
     const int warps = blockDim.x >> 5;
     const int lane = threadIdx.x & 31;
     for (int b = blockIdx.x * warps + (threadIdx.x >> 5); b < g.nbricks; b += gridDim.x * warps) {
-        const float4 *rp = records + (size_t)table[b] * R;
+        const uint32_t slot = table[b];
+        const float4 *rp = records + (size_t)slot * R;
         float lo = __int_as_float(0x7f800000), hi = -lo;
         bool nan = false;
         for (int i = lane; i < R; i += 32) {
@@ -191,7 +192,9 @@ __global__ void brick_minmax_kernel(BrickGeometry g, const uint32_t *__restrict_
             hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
         }
         nan = __any_sync(0xffffffffu, nan);
-        if (lane == 0) mm[b] = nan ? make_float2(__int_as_float(0x7fc00000), 0.0f) : make_float2(lo, hi);
+        if (lane == 0)
+            bricks[b] = nan ? make_uint4(slot, 0x7fc00000u, 0u, 0u)
+                            : make_uint4(slot, __float_as_uint(lo), __float_as_uint(hi), 0u);
     }
 }
 
@@ -230,7 +233,7 @@ uint32_t spread3(uint32_t v) {  // 10 bits -> every third bit
 
 template <typename T, int LOG2B>
 cudaError_t build_typed(const BrickGeometry &g, const void *vol, const int dims[3], const float *nrm,
-                        int normals_mode, const uint32_t *table, float4 *records, float2 *minmax,
+                        int normals_mode, const uint32_t *table, float4 *records, uint4 *bricks,
                         cudaStream_t st) {
     constexpr int R = brick_records(LOG2B);
     const long long total = (long long)g.nbricks * R;
@@ -240,21 +243,21 @@ cudaError_t build_typed(const BrickGeometry &g, const void *vol, const int dims[
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     int mblocks = std::max(1, std::min((g.nbricks + 7) / 8, 152 * 16));
-    brick_minmax_kernel<LOG2B><<<mblocks, 256, 0, st>>>(g, table, records, minmax);
+    brick_minmax_kernel<LOG2B><<<mblocks, 256, 0, st>>>(g, table, records, bricks);
     return cudaGetLastError();
 }
 
 template <int LOG2B>
 cudaError_t build_log2(const BrickGeometry &g, int dtype, const void *vol, const int dims[3],
                        const float *nrm, int normals_mode, const uint32_t *table, float4 *records,
-                       float2 *minmax, cudaStream_t st) {
+                       uint4 *bricks, cudaStream_t st) {
     switch (dtype) {
     case PVR_U8:
-        return build_typed<uint8_t, LOG2B>(g, vol, dims, nrm, normals_mode, table, records, minmax, st);
+        return build_typed<uint8_t, LOG2B>(g, vol, dims, nrm, normals_mode, table, records, bricks, st);
     case PVR_F16:
-        return build_typed<__half, LOG2B>(g, vol, dims, nrm, normals_mode, table, records, minmax, st);
+        return build_typed<__half, LOG2B>(g, vol, dims, nrm, normals_mode, table, records, bricks, st);
     default:
-        return build_typed<float, LOG2B>(g, vol, dims, nrm, normals_mode, table, records, minmax, st);
+        return build_typed<float, LOG2B>(g, vol, dims, nrm, normals_mode, table, records, bricks, st);
     }
 }
 
@@ -290,11 +293,11 @@ std::vector<uint32_t> morton_slots(const BrickGeometry &g) {
 
 cudaError_t launch_build_records(const BrickGeometry &g, int dtype, const void *vol, const int dims[3],
                                  const float *nrm, int normals_mode, const uint32_t *table,
-                                 float4 *records, float2 *minmax, cudaStream_t st) {
+                                 float4 *records, uint4 *bricks, cudaStream_t st) {
     switch (g.log2b) {
-    case 2: return build_log2<2>(g, dtype, vol, dims, nrm, normals_mode, table, records, minmax, st);
-    case 4: return build_log2<4>(g, dtype, vol, dims, nrm, normals_mode, table, records, minmax, st);
-    default: return build_log2<3>(g, dtype, vol, dims, nrm, normals_mode, table, records, minmax, st);
+    case 2: return build_log2<2>(g, dtype, vol, dims, nrm, normals_mode, table, records, bricks, st);
+    case 4: return build_log2<4>(g, dtype, vol, dims, nrm, normals_mode, table, records, bricks, st);
+    default: return build_log2<3>(g, dtype, vol, dims, nrm, normals_mode, table, records, bricks, st);
     }
 }
 

@@ -3,11 +3,9 @@
 
 namespace pvr {
 
-cudaError_t launch_march_batch_b3(const Tuning &t, const BatchHeader *hdr, const int *tile_bases,
-                                  const JobDesc *jobs, int *work, int grid, int lut_smem_entries,
-                                  cudaStream_t st) {
-    return launch_batch_log2<3>(t, hdr, tile_bases, jobs, work, grid, lut_smem_entries, st);
-}
+const void *batch_kernel_b3(const Tuning &t) { return batch_kernel_log2<3>(t); }
+
+const void *single_kernel_b3(const Tuning &t) { return single_kernel_log2<3>(t); }
 
 int max_batch_blocks_b3(const Tuning &t, int lut_smem_entries) {
     return max_blocks_log2<3>(t, lut_smem_entries);

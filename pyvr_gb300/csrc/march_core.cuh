@@ -3,10 +3,11 @@
 //
 // Work is a queue of pixel tiles over every job of the batch (one job =
 // one render with its own volume, LUT, camera, light, config and size).
-// Each 256-thread block pops a tile with one atomic, caches the tile's job
-// descriptor in shared memory when the job changes and stages that job's
-// RGBA LUT (plus the LUT's "clear entry" prefix counts) next to it, then
-// marches one ray per thread.  Warps cover 8x4-pixel sub-tiles so the rays
+// The job table is the kernel's parameter block, so frame constants are
+// read through the constant cache as in a single-render kernel.  Each
+// 256-thread block pops a tile with one atomic, stages the tile's RGBA LUT
+// (plus the LUT's "clear entry" prefix counts) in shared memory when the
+// job changes, then marches one ray per thread.  Warps cover 8x4-pixel sub-tiles so the rays
 // of a warp are spatially close and their trilinear footprints share cache
 // lines.  Voxels and normals are read from the bricked 16-byte texel
 // records of layout.cu: each sample is 8 vector loads at fixed offsets from
@@ -153,6 +154,7 @@ __device__ __forceinline__ uint32_t blend_rgba8(float2 rg, float2 ba) {
 }
 
 // Is a sample of this brick exactly transparent under the job's LUT?
+// m = the brick's (min, max) stored values.
 template <bool SMEM_LUT>
 __device__ __forceinline__ bool brick_clear(const MarchFrame &f, float2 m, const int *prefix) {
     if (!(m.x == m.x)) return false;  // NaN in the brick
@@ -212,8 +214,11 @@ __device__ __forceinline__ void march_ray(const JobDesc &job, int px, int py, co
                 const int id = ((kx >> LOG2B) * nb1 + (ky >> LOG2B)) * nb2 + (kz >> LOG2B);
                 if (id != cur_brick) {
                     cur_brick = id;
-                    bp = job.records + (size_t)__ldg(job.table + id) * RECS;
-                    clear = job.skip && brick_clear<SMEM_LUT>(f, __ldg(job.minmax + id), prefix);
+                    const uint4 bi = __ldg(job.bricks + id);
+                    bp = job.records + (size_t)bi.x * RECS;
+                    clear = job.skip &&
+                            brick_clear<SMEM_LUT>(f, make_float2(__uint_as_float(bi.y), __uint_as_float(bi.z)),
+                                                  prefix);
                 }
                 if (!clear) {
                     ++n_shaded;
@@ -266,87 +271,108 @@ __device__ __forceinline__ void march_tile(const JobDesc &job, int px, int py, c
     }
 }
 
-// Persistent batch kernel.  Dynamic shared memory: lut_smem_entries float4
-// LUT entries followed by lut_smem_entries + 1 prefix counts.
+// Persistent batch kernel.  The job table is the kernel's own parameter
+// block (read through the constant cache).  Dynamic shared memory:
+// p.lut_smem_entries float4 LUT entries followed by as many + 1 prefix counts.
 template <int LOG2B, int UNROLL>
-__global__ void __launch_bounds__(kBatchThreads, 4)
-march_batch_kernel(const BatchHeader *__restrict__ hdr, const int *__restrict__ tile_bases,
-                   const JobDesc *__restrict__ jobs, int *__restrict__ work, int lut_smem_entries) {
+__global__ void __launch_bounds__(kBatchThreads, 5)
+march_batch_kernel(const __grid_constant__ BatchParams p) {
     extern __shared__ float4 s_dyn[];
     float4 *s_lut = s_dyn;
-    int *s_prefix = reinterpret_cast<int *>(s_dyn + lut_smem_entries);
-    __shared__ JobDesc s_job;
+    int *s_prefix = reinterpret_cast<int *>(s_dyn + p.lut_smem_entries);
     __shared__ int s_tile, s_job_idx;
-    const int njobs = hdr->njobs, total = hdr->total_tiles;
-    const int tile_w = hdr->tile_w, tile_h = hdr->tile_h;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int warps_x = tile_w >> 3;
+    const int warps_x = p.tile_w >> 3;
     const int sub_x = (warp % warps_x) * 8 + (lane & 7);
     const int sub_y = (warp / warps_x) * 4 + (lane >> 3);
     int cur_job = -1;
     bool lut_in_smem = false;
     for (;;) {
         if (threadIdx.x == 0) {
-            const int t = atomicAdd(work, 1);
-            int lo = 0, hi = njobs - 1;  // last job whose first tile is <= t
+            const int t = atomicAdd(p.work, 1);
+            int lo = 0, hi = p.njobs - 1;  // last job whose first tile is <= t
             while (lo < hi) {
                 const int mid = (lo + hi + 1) >> 1;
-                if (tile_bases[mid] <= t) lo = mid; else hi = mid - 1;
+                if (p.tile_base[mid] <= t) lo = mid; else hi = mid - 1;
             }
             s_tile = t;
             s_job_idx = lo;
         }
         __syncthreads();
         const int t = s_tile, j = s_job_idx;
-        if (t >= total) break;
+        if (t >= p.total_tiles) break;
+        const JobDesc &job = p.jobs[j];
         if (j != cur_job) {
-            // cache the job descriptor and stage its LUT
-            const int *src = reinterpret_cast<const int *>(jobs + j);
-            int *dst = reinterpret_cast<int *>(&s_job);
-            for (int w = threadIdx.x; w < (int)(sizeof(JobDesc) / 4); w += kBatchThreads) dst[w] = src[w];
-            __syncthreads();
-            lut_in_smem = s_job.f.lut_size <= lut_smem_entries;
+            // stage the job's LUT (the previous tile's readers passed the
+            // barrier at the end of the last round)
+            lut_in_smem = job.f.lut_size <= p.lut_smem_entries;
             if (lut_in_smem) {
-                for (int k = threadIdx.x; k < s_job.f.lut_size; k += kBatchThreads) s_lut[k] = s_job.lut[k];
-                for (int k = threadIdx.x; k <= s_job.f.lut_size; k += kBatchThreads) s_prefix[k] = s_job.prefix[k];
+                for (int k = threadIdx.x; k < job.f.lut_size; k += kBatchThreads) s_lut[k] = job.lut[k];
+                for (int k = threadIdx.x; k <= job.f.lut_size; k += kBatchThreads) s_prefix[k] = job.prefix[k];
             }
             __syncthreads();
             cur_job = j;
         }
-        const int local = t - s_job.tile_base;
-        const int px = (local % s_job.tiles_x) * tile_w + sub_x;
-        const int py = (local / s_job.tiles_x) * tile_h + sub_y;
-        if (s_job.normals) {
-            if (lut_in_smem) march_tile<LOG2B, UNROLL, true, true>(s_job, px, py, s_lut, s_prefix, lane);
-            else march_tile<LOG2B, UNROLL, true, false>(s_job, px, py, s_job.lut, s_job.prefix, lane);
+        const int local = t - job.tile_base;
+        const int px = (local % job.tiles_x) * p.tile_w + sub_x;
+        const int py = (local / job.tiles_x) * p.tile_h + sub_y;
+        if (job.normals) {
+            if (lut_in_smem) march_tile<LOG2B, UNROLL, true, true>(job, px, py, s_lut, s_prefix, lane);
+            else march_tile<LOG2B, UNROLL, true, false>(job, px, py, job.lut, job.prefix, lane);
         } else {
-            if (lut_in_smem) march_tile<LOG2B, UNROLL, false, true>(s_job, px, py, s_lut, s_prefix, lane);
-            else march_tile<LOG2B, UNROLL, false, false>(s_job, px, py, s_job.lut, s_job.prefix, lane);
+            if (lut_in_smem) march_tile<LOG2B, UNROLL, false, true>(job, px, py, s_lut, s_prefix, lane);
+            else march_tile<LOG2B, UNROLL, false, false>(job, px, py, job.lut, job.prefix, lane);
         }
-        __syncthreads();  // s_tile / s_job are rewritten next round
+        __syncthreads();  // s_tile / the staged LUT are rewritten next round
+    }
+}
+
+// Single-job kernel: one block per tile of one render; the job descriptor
+// is the parameter block itself (static offsets), as in a plain frame kernel.
+template <int LOG2B, int UNROLL>
+__global__ void __launch_bounds__(kBatchThreads, 5)
+march_single_kernel(const __grid_constant__ SingleParams p) {
+    extern __shared__ float4 s_dyn[];
+    float4 *s_lut = s_dyn;
+    int *s_prefix = reinterpret_cast<int *>(s_dyn + p.lut_smem_entries);
+    const JobDesc &job = p.job;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int warps_x = p.tile_w >> 3;
+    const bool lut_in_smem = job.f.lut_size <= p.lut_smem_entries;
+    if (lut_in_smem) {
+        for (int k = threadIdx.x; k < job.f.lut_size; k += kBatchThreads) s_lut[k] = job.lut[k];
+        for (int k = threadIdx.x; k <= job.f.lut_size; k += kBatchThreads) s_prefix[k] = job.prefix[k];
+        __syncthreads();
+    }
+    const int t = blockIdx.x;
+    const int px = (t % job.tiles_x) * p.tile_w + (warp % warps_x) * 8 + (lane & 7);
+    const int py = (t / job.tiles_x) * p.tile_h + (warp / warps_x) * 4 + (lane >> 3);
+    if (job.normals) {
+        if (lut_in_smem) march_tile<LOG2B, UNROLL, true, true>(job, px, py, s_lut, s_prefix, lane);
+        else march_tile<LOG2B, UNROLL, true, false>(job, px, py, job.lut, job.prefix, lane);
+    } else {
+        if (lut_in_smem) march_tile<LOG2B, UNROLL, false, true>(job, px, py, s_lut, s_prefix, lane);
+        else march_tile<LOG2B, UNROLL, false, false>(job, px, py, job.lut, job.prefix, lane);
     }
 }
 
 template <int LOG2B>
-cudaError_t launch_batch_log2(const Tuning &t, const BatchHeader *hdr, const int *tile_bases,
-                              const JobDesc *jobs, int *work, int grid, int lut_smem_entries,
-                              cudaStream_t st) {
-    const size_t shm = (size_t)lut_smem_entries * sizeof(float4) + (size_t)(lut_smem_entries + 1) * sizeof(int);
-    if (t.steps_per_iter >= 4)
-        march_batch_kernel<LOG2B, 4><<<grid, kBatchThreads, shm, st>>>(hdr, tile_bases, jobs, work, lut_smem_entries);
-    else
-        march_batch_kernel<LOG2B, 1><<<grid, kBatchThreads, shm, st>>>(hdr, tile_bases, jobs, work, lut_smem_entries);
-    return cudaGetLastError();
+const void *single_kernel_log2(const Tuning &t) {
+    if (t.steps_per_iter >= 4) return (const void *)march_single_kernel<LOG2B, 4>;
+    return (const void *)march_single_kernel<LOG2B, 1>;
+}
+
+template <int LOG2B>
+const void *batch_kernel_log2(const Tuning &t) {
+    if (t.steps_per_iter >= 4) return (const void *)march_batch_kernel<LOG2B, 4>;
+    return (const void *)march_batch_kernel<LOG2B, 1>;
 }
 
 template <int LOG2B>
 int max_blocks_log2(const Tuning &t, int lut_smem_entries) {
-    const size_t shm = (size_t)lut_smem_entries * sizeof(float4) + (size_t)(lut_smem_entries + 1) * sizeof(int);
     int n = 0;
-    if (t.steps_per_iter >= 4)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, march_batch_kernel<LOG2B, 4>, kBatchThreads, shm);
-    else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, march_batch_kernel<LOG2B, 1>, kBatchThreads, shm);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel_log2<LOG2B>(t), kBatchThreads,
+                                                  batch_smem_bytes(lut_smem_entries));
     return n;
 }
 

@@ -37,9 +37,11 @@ std::vector<uint32_t> morton_slots(const BrickGeometry &g);
 
 // normals_mode: 0 none, 1 from `nrm` (float32 (D,H,W,3)), 2 computed on the
 // device from the stored values (numpy.gradient semantics).
+// bricks[b] = {record slot, min, max (float bits), 0}: what the march needs
+// when a ray enters brick b, in one 16-byte load.
 cudaError_t launch_build_records(const BrickGeometry &g, int dtype, const void *vol, const int dims[3],
                                  const float *nrm, int normals_mode, const uint32_t *table,
-                                 float4 *records, float2 *minmax, cudaStream_t st);
+                                 float4 *records, uint4 *bricks, cudaStream_t st);
 cudaError_t launch_read_normals(const BrickGeometry &g, const int dims[3], const uint32_t *table,
                                 const float4 *records, float *out, cudaStream_t st);
 
@@ -47,8 +49,7 @@ cudaError_t launch_read_normals(const BrickGeometry &g, const int dims[3], const
 struct JobDesc {
     MarchFrame f;
     const float4 *records;
-    const uint32_t *table;
-    const float2 *minmax;
+    const uint4 *bricks;  // {slot, min bits, max bits, 0} per brick
     const float4 *lut;
     const int *prefix;  // prefix[i] = LUT entries before i that are not exactly clear
     uint32_t *out8;
@@ -56,14 +57,29 @@ struct JobDesc {
     unsigned long long *counters;  // [in-box samples, shaded samples] or null
     int tiles_x, tiles_y, tile_base;
     int normals;
-    int skip;  // empty-space skipping allowed (finite light terms)
-    int pad_[3];
+    int skip;  // empty-space test on: the LUT has a clear entry and the light terms are finite
+    int pad_[4];
 };
 
-struct BatchHeader {
+// Kernel parameters of one persistent launch: up to kMaxLaunchJobs job
+// descriptors passed by value (read through the constant cache).
+constexpr int kMaxLaunchJobs = 96;
+struct BatchParams {
     int njobs;
     int total_tiles;
     int tile_w, tile_h;
+    int lut_smem_entries;
+    int *work;
+    int tile_base[kMaxLaunchJobs];
+    JobDesc jobs[kMaxLaunchJobs];
+};
+static_assert(sizeof(BatchParams) <= 32000, "kernel parameter block too large");
+
+// Kernel parameters of a launch with a single job (one block per tile).
+struct SingleParams {
+    JobDesc job;
+    int tile_w, tile_h;
+    int lut_smem_entries;
 };
 
 constexpr int kBatchThreads = 256;
@@ -77,10 +93,11 @@ struct Tuning {
     int blocks_per_sm = 4;
 };
 
-// Persistent batch march (march_core.cuh), one instantiation per brick size.
-cudaError_t launch_march_batch(int log2b, const Tuning &t, const BatchHeader *hdr,
-                               const int *tile_bases, const JobDesc *jobs, int *work, int grid,
-                               int lut_smem_entries, cudaStream_t st);
+// Persistent batch march (march_core.cuh), one instantiation per brick size:
+// the kernel function for a tuning, and the blocks of it that fit on an SM.
+const void *batch_kernel(int log2b, const Tuning &t);
+const void *single_kernel(int log2b, const Tuning &t);
+size_t batch_smem_bytes(int lut_smem_entries);
 int max_batch_blocks_per_sm(int log2b, const Tuning &t, int lut_smem_entries);
 
 }  // namespace pvr
@@ -103,8 +120,8 @@ struct pvr_volume {
     pvr::BrickGeometry geo = {};
     float4 *d_records = nullptr;
     size_t records_bytes = 0;
-    uint32_t *d_table = nullptr;
-    float2 *d_minmax = nullptr;
+    uint32_t *d_table = nullptr;  // brick -> record slot
+    uint4 *d_bricks = nullptr;    // brick -> {slot, min, max}
     bool layout_ready = false;
 };
 
@@ -113,6 +130,7 @@ struct pvr_lut {
     int size = 0, cap = 0;
     float4 *d_lut = nullptr;
     int *d_prefix = nullptr;
+    bool has_clear = false;  // some entry has alpha exactly 0 and a finite colour
 };
 
 namespace pvr {

@@ -79,10 +79,10 @@ int ensure_volume_layout(pvr_volume *v, cudaStream_t st) {
     if (v->layout_ready) return PVR_OK;
     cudaFree(v->d_records);
     cudaFree(v->d_table);
-    cudaFree(v->d_minmax);
+    cudaFree(v->d_bricks);
     v->d_records = nullptr;
     v->d_table = nullptr;
-    v->d_minmax = nullptr;
+    v->d_bricks = nullptr;
     v->records_bytes = 0;
     v->geo = make_brick_geometry(v->dims, v->log2b);
     std::vector<uint32_t> table = morton_slots(v->geo);
@@ -90,11 +90,11 @@ int ensure_volume_layout(pvr_volume *v, cudaStream_t st) {
     PVR_CUDA(cudaMalloc(&v->d_records, nrec * sizeof(float4)));
     v->records_bytes = nrec * sizeof(float4);
     PVR_CUDA(cudaMalloc(&v->d_table, table.size() * sizeof(uint32_t)));
-    PVR_CUDA(cudaMalloc(&v->d_minmax, table.size() * sizeof(float2)));
+    PVR_CUDA(cudaMalloc(&v->d_bricks, table.size() * sizeof(uint4)));
     PVR_CUDA(cudaMemcpyAsync(v->d_table, table.data(), table.size() * sizeof(uint32_t),
                              cudaMemcpyHostToDevice, st));
     PVR_CUDA(launch_build_records(v->geo, v->dtype, v->d_vol, v->dims, v->d_nrm, v->normals_mode,
-                                  v->d_table, v->d_records, v->d_minmax, st));
+                                  v->d_table, v->d_records, v->d_bricks, st));
     PVR_CUDA(cudaStreamSynchronize(st));  // `table` leaves scope
     cudaFree(v->d_nrm);  // given normals now live in the records
     v->d_nrm = nullptr;
@@ -142,8 +142,7 @@ int fill_job(const pvr_job &j, int tile_w, int tile_h, JobDesc &out) {
     f.lut_size = j.lut->size;
     f.flut_size = (float)j.lut->size;
     out.records = v.d_records;
-    out.table = v.d_table;
-    out.minmax = v.d_minmax;
+    out.bricks = v.d_bricks;
     out.lut = j.lut->d_lut;
     out.prefix = j.lut->d_prefix;
     out.out8 = (uint32_t *)j.d_rgba8;
@@ -152,7 +151,7 @@ int fill_job(const pvr_job &j, int tile_w, int tile_h, JobDesc &out) {
     out.tiles_x = (j.width + tile_w - 1) / tile_w;
     out.tiles_y = (j.height + tile_h - 1) / tile_h;
     out.normals = v.normals_mode != PVR_NORMALS_NONE;
-    out.skip = std::isfinite(j.ambient) && std::isfinite(j.diffuse);
+    out.skip = j.lut->has_clear && std::isfinite(j.ambient) && std::isfinite(j.diffuse);
     return PVR_OK;
 }
 
@@ -209,7 +208,7 @@ int pvr_volume_create(const void *data, int dtype, int d, int h, int w, float va
         cudaFree(v->d_nrm);
         cudaFree(v->d_records);
         cudaFree(v->d_table);
-        cudaFree(v->d_minmax);
+        cudaFree(v->d_bricks);
         delete v;
         return rc;
     };
@@ -236,7 +235,7 @@ int pvr_volume_destroy(pvr_volume *v) {
     cudaFree(v->d_nrm);
     cudaFree(v->d_records);
     cudaFree(v->d_table);
-    cudaFree(v->d_minmax);
+    cudaFree(v->d_bricks);
     delete v;
     return PVR_OK;
 }
@@ -244,7 +243,7 @@ int pvr_volume_destroy(pvr_volume *v) {
 int pvr_volume_device_bytes(const pvr_volume *v, long long *bytes) {
     if (!v || !bytes) return fail(PVR_ERR_VALUE, "NULL argument");
     *bytes = (long long)(v->vol_bytes + v->records_bytes +
-                         (size_t)v->geo.nbricks * (sizeof(uint32_t) + sizeof(float2)));
+                         (size_t)v->geo.nbricks * (sizeof(uint32_t) + sizeof(uint4)));
     return PVR_OK;
 }
 
@@ -302,6 +301,7 @@ int pvr_lut_update(pvr_lut *l, const float *rgba, int size) {
     PVR_CUDA(cudaMemcpy(l->d_lut, rgba, (size_t)size * sizeof(float4), cudaMemcpyHostToDevice));
     PVR_CUDA(cudaMemcpy(l->d_prefix, prefix.data(), (size_t)(size + 1) * sizeof(int), cudaMemcpyHostToDevice));
     l->size = size;
+    l->has_clear = prefix[size] < size;
     return PVR_OK;
 }
 

@@ -142,3 +142,34 @@ def frame_inputs(volume: Volume, camera, light, config, lut: np.ndarray, width: 
                 step_size=config.step_size, reference_step_size=config.reference_step_size,
                 max_steps=config.max_steps, light_pos=light.position, light_target=light.target,
                 ambient=light.ambient_intensity, diffuse=light.diffuse_intensity)
+
+
+def config_batching(n: int = 64, max_dim: int = 384, resolutions=(128, 256, 512, 1024)):
+    """n uneven renders: per instance i (seed i) volume extents drawn
+    log-uniformly from 32..max_dim per axis (non-cubic), storage uniform over
+    uint8/float16/float32, value noise, resolution uniform over the given
+    squares, a random camera on a sphere of radius 2.5-4 around the box, and
+    a random TF (4-12 opacity points, one of the 12 stand-in colour maps).
+    Normals are left to the device (numpy.gradient semantics)."""
+    scenes = []
+    for i in range(n):
+        rng = np.random.default_rng(i)
+        dims = tuple(int(round(x)) for x in np.exp(rng.uniform(np.log(32), np.log(max_dim), 3)))
+        dtype = ["u8", "f16", "f32"][int(rng.integers(0, 3))]
+        res = int(resolutions[int(rng.integers(0, len(resolutions)))])
+        radius = float(rng.uniform(2.5, 4.0))
+        v = rng.normal(size=3)
+        v /= np.linalg.norm(v)
+        az = float(np.arctan2(v[1], v[0]))
+        el = float(np.arcsin(np.clip(v[2], -1, 1)))
+        otf = random_opacity(rng, int(rng.integers(4, 13)), 0.3)
+        ctf = standin_colormap(int(rng.integers(0, N_STANDIN_COLORMAPS)))
+        data = to_storage(value_noise(dims, seed=i), dtype)
+        vol = Volume(data=data, min_bounds=np.array([-1.0, -1.0, -1.0], np.float32),
+                     max_bounds=np.array([1.0, 1.0, 1.0], np.float32))
+        cam = Camera.from_spherical(target=np.zeros(3, np.float32), azimuth=az, elevation=el, roll=0.0,
+                                    distance=radius)
+        scenes.append(dict(volume=vol, dtype=dtype, value_scale=(1.0 / 255.0 if dtype == "u8" else 1.0),
+                           camera=cam, light=Light.directional([1, -1, 0], 0.2, 0.8), ctf=ctf, otf=otf,
+                           config=RenderConfig.balanced(), width=res, height=res))
+    return scenes
