@@ -159,7 +159,11 @@ int pvr_frame_constants(const float view[16], const float proj[16], const float 
 int pvr_volume_create(const void *data, int dtype, int d, int h, int w, float value_scale,
                       const float min_bounds[3], const float max_bounds[3], const float *normals,
                       int normals_mode, int brick_log2, pvr_volume **out);
-int pvr_volume_destroy(pvr_volume *v);
+int pvr_volume_destroy(pvr_volume *v);   /* waits for the whole device first */
+/* Free the volume's memory in order on `stream` without waiting: the caller
+ * makes `stream` wait for every batch that reads the volume.  The handle is
+ * invalid on return. */
+int pvr_volume_release(pvr_volume *v, void *stream);
 int pvr_volume_device_bytes(const pvr_volume *v, long long *bytes);
 /* The float32 (D,H,W,3) normals held in the records (host buffer). */
 int pvr_volume_read_normals(const pvr_volume *v, float *normals_out);

@@ -114,6 +114,7 @@ SIGNATURES = {
     "pvr_set_tuning": (_I, [_VP, _VP]),
     "pvr_volume_create": (_I, [_VP, _I, _I, _I, _I, _F, _FP, _FP, _VP, _I, _I, ctypes.POINTER(_VP)]),
     "pvr_volume_destroy": (_I, [_VP]),
+    "pvr_volume_release": (_I, [_VP, _VP]),
     "pvr_volume_device_bytes": (_I, [_VP, ctypes.POINTER(_LL)]),
     "pvr_volume_read_normals": (_I, [_VP, _VP]),
     "pvr_lut_create": (_I, [_VP, _I, ctypes.POINTER(_VP)]),

@@ -183,10 +183,12 @@ int pvr_load_volume(pvr_renderer *r, const void *data, int dtype, int d, int h, 
         v->bmax[a] = max_bounds[a];
     }
     v->vol_bytes = (size_t)d * h * w * dtype_size(dtype);
-    cudaError_t e = cudaMalloc(&v->d_vol, v->vol_bytes);
-    if (e == cudaSuccess) e = cudaMemcpy(v->d_vol, data, v->vol_bytes, cudaMemcpyHostToDevice);
+    cudaError_t e = pvr::vol_alloc(&v->d_vol, v->vol_bytes, r->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(v->d_vol, data, v->vol_bytes, cudaMemcpyHostToDevice, r->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(r->stream);
     if (e != cudaSuccess) {
-        cudaFree(v->d_vol);
+        pvr::vol_free(v->d_vol, r->stream);
+        cudaStreamSynchronize(r->stream);
         delete v;
         return pvr::cuda_fail(e, "upload volume");
     }
@@ -209,10 +211,11 @@ int pvr_load_normals(pvr_renderer *r, const float *normals) {
     if (int rc = quiesce(r)) return rc;
     pvr_volume *v = r->vol;
     const size_t bytes = (size_t)v->dims[0] * v->dims[1] * v->dims[2] * 3 * sizeof(float);
-    cudaFree(v->d_nrm);
+    pvr::vol_free(v->d_nrm, r->stream);
     v->d_nrm = nullptr;
-    PVR_CUDA(cudaMalloc(&v->d_nrm, bytes));
-    PVR_CUDA(cudaMemcpy(v->d_nrm, normals, bytes, cudaMemcpyHostToDevice));
+    PVR_CUDA(pvr::vol_alloc((void **)&v->d_nrm, bytes, r->stream));
+    PVR_CUDA(cudaMemcpyAsync(v->d_nrm, normals, bytes, cudaMemcpyHostToDevice, r->stream));
+    PVR_CUDA(cudaStreamSynchronize(r->stream));
     v->normals_mode = PVR_NORMALS_GIVEN;
     v->layout_ready = false;
     return PVR_OK;
@@ -227,7 +230,7 @@ int pvr_compute_normals(pvr_renderer *r) {
                                    "at least (edge_order + 1) elements are required.");
     DeviceScope ds(r->device);
     if (int rc = quiesce(r)) return rc;
-    cudaFree(v->d_nrm);
+    pvr::vol_free(v->d_nrm, r->stream);
     v->d_nrm = nullptr;
     v->normals_mode = PVR_NORMALS_DEVICE;
     v->layout_ready = false;

@@ -138,6 +138,9 @@ namespace pvr {
 int fail(int code, const char *fmt, ...);
 int cuda_fail(cudaError_t e, const char *what);
 int ensure_volume_layout(pvr_volume *v, cudaStream_t st);
+cudaError_t vol_alloc(void **p, size_t bytes, cudaStream_t st);
+void vol_free(void *p, cudaStream_t st);
+void free_volume_buffers(pvr_volume *v, cudaStream_t st);
 bool invert_gl(const float gl[16], double inv[16]);
 void light_direction(const float pos[3], const float target[3], float out[3]);
 int fill_job(const pvr_job &j, int tile_w, int tile_h, JobDesc &out);

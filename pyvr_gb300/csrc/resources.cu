@@ -74,12 +74,48 @@ void light_direction(const float pos[3], const float target[3], float out[3]) {
     for (int a = 0; a < 3; ++a) out[a] = l[a] * li;
 }
 
+// Volume memory comes from the stream-ordered allocator: unlike
+// cudaMalloc / cudaFree it is no synchronisation point between streams, so
+// loading or evicting a volume does not stall renders running meanwhile.
+// The pool keeps freed memory for reuse instead of returning it at every
+// synchronisation.
+cudaError_t vol_alloc(void **p, size_t bytes, cudaStream_t st) {
+    static bool pool_configured = false;
+    if (!pool_configured) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+            uint64_t keep = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+        pool_configured = true;
+    }
+    return cudaMallocAsync(p, bytes, st);
+}
+
+void vol_free(void *p, cudaStream_t st) {
+    if (p) cudaFreeAsync(p, st);
+}
+
+void free_volume_buffers(pvr_volume *v, cudaStream_t st) {
+    vol_free(v->d_vol, st);
+    vol_free(v->d_nrm, st);
+    vol_free(v->d_records, st);
+    vol_free(v->d_table, st);
+    vol_free(v->d_bricks, st);
+    v->d_vol = v->d_nrm = nullptr;
+    v->d_records = nullptr;
+    v->d_table = nullptr;
+    v->d_bricks = nullptr;
+}
+
 // Records, brick table and value ranges of a volume (once per volume).
 int ensure_volume_layout(pvr_volume *v, cudaStream_t st) {
     if (v->layout_ready) return PVR_OK;
-    cudaFree(v->d_records);
-    cudaFree(v->d_table);
-    cudaFree(v->d_bricks);
+    vol_free(v->d_records, st);
+    vol_free(v->d_table, st);
+    vol_free(v->d_bricks, st);
     v->d_records = nullptr;
     v->d_table = nullptr;
     v->d_bricks = nullptr;
@@ -87,17 +123,17 @@ int ensure_volume_layout(pvr_volume *v, cudaStream_t st) {
     v->geo = make_brick_geometry(v->dims, v->log2b);
     std::vector<uint32_t> table = morton_slots(v->geo);
     const size_t nrec = (size_t)v->geo.nbricks * brick_records(v->log2b);
-    PVR_CUDA(cudaMalloc(&v->d_records, nrec * sizeof(float4)));
+    PVR_CUDA(vol_alloc((void **)&v->d_records, nrec * sizeof(float4), st));
     v->records_bytes = nrec * sizeof(float4);
-    PVR_CUDA(cudaMalloc(&v->d_table, table.size() * sizeof(uint32_t)));
-    PVR_CUDA(cudaMalloc(&v->d_bricks, table.size() * sizeof(uint4)));
+    PVR_CUDA(vol_alloc((void **)&v->d_table, table.size() * sizeof(uint32_t), st));
+    PVR_CUDA(vol_alloc((void **)&v->d_bricks, table.size() * sizeof(uint4), st));
     PVR_CUDA(cudaMemcpyAsync(v->d_table, table.data(), table.size() * sizeof(uint32_t),
                              cudaMemcpyHostToDevice, st));
     PVR_CUDA(launch_build_records(v->geo, v->dtype, v->d_vol, v->dims, v->d_nrm, v->normals_mode,
                                   v->d_table, v->d_records, v->d_bricks, st));
-    PVR_CUDA(cudaStreamSynchronize(st));  // `table` leaves scope
-    cudaFree(v->d_nrm);  // given normals now live in the records
+    vol_free(v->d_nrm, st);  // given normals now live in the records
     v->d_nrm = nullptr;
+    PVR_CUDA(cudaStreamSynchronize(st));  // `table` leaves scope; ready for any stream
     v->layout_ready = true;
     return PVR_OK;
 }
@@ -203,27 +239,33 @@ int pvr_volume_create(const void *data, int dtype, int d, int h, int w, float va
         v->bmax[a] = max_bounds[a];
     }
     const size_t nvox = (size_t)d * h * w;
+    // a stream of its own: the load runs beside renders on other streams
+    cudaStream_t st = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete v;
+        return pvr::cuda_fail(e, "cudaStreamCreateWithFlags");
+    }
     auto bail = [&](int rc) {
-        cudaFree(v->d_vol);
-        cudaFree(v->d_nrm);
-        cudaFree(v->d_records);
-        cudaFree(v->d_table);
-        cudaFree(v->d_bricks);
+        pvr::free_volume_buffers(v, st);
+        cudaStreamSynchronize(st);
+        cudaStreamDestroy(st);
         delete v;
         return rc;
     };
-    cudaError_t e = cudaMalloc(&v->d_vol, nvox * dtype_size(dtype));
-    if (e != cudaSuccess) return bail(pvr::cuda_fail(e, "cudaMalloc(volume)"));
+    e = pvr::vol_alloc(&v->d_vol, nvox * dtype_size(dtype), st);
+    if (e != cudaSuccess) return bail(pvr::cuda_fail(e, "allocate volume"));
     v->vol_bytes = nvox * dtype_size(dtype);
-    e = cudaMemcpy(v->d_vol, data, v->vol_bytes, cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) return bail(pvr::cuda_fail(e, "cudaMemcpy(volume)"));
+    e = cudaMemcpyAsync(v->d_vol, data, v->vol_bytes, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return bail(pvr::cuda_fail(e, "upload volume"));
     if (normals_mode == PVR_NORMALS_GIVEN) {
-        e = cudaMalloc(&v->d_nrm, nvox * 3 * sizeof(float));
-        if (e != cudaSuccess) return bail(pvr::cuda_fail(e, "cudaMalloc(normals)"));
-        e = cudaMemcpy(v->d_nrm, normals, nvox * 3 * sizeof(float), cudaMemcpyHostToDevice);
-        if (e != cudaSuccess) return bail(pvr::cuda_fail(e, "cudaMemcpy(normals)"));
+        e = pvr::vol_alloc((void **)&v->d_nrm, nvox * 3 * sizeof(float), st);
+        if (e != cudaSuccess) return bail(pvr::cuda_fail(e, "allocate normals"));
+        e = cudaMemcpyAsync(v->d_nrm, normals, nvox * 3 * sizeof(float), cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess) return bail(pvr::cuda_fail(e, "upload normals"));
     }
-    if (int rc = pvr::ensure_volume_layout(v, 0)) return bail(rc);
+    if (int rc = pvr::ensure_volume_layout(v, st)) return bail(rc);
+    cudaStreamDestroy(st);
     *out = v;
     return PVR_OK;
 }
@@ -231,11 +273,15 @@ int pvr_volume_create(const void *data, int dtype, int d, int h, int w, float va
 int pvr_volume_destroy(pvr_volume *v) {
     if (!v) return PVR_OK;
     cudaDeviceSynchronize();  // no batch may still read it
-    cudaFree(v->d_vol);
-    cudaFree(v->d_nrm);
-    cudaFree(v->d_records);
-    cudaFree(v->d_table);
-    cudaFree(v->d_bricks);
+    pvr::free_volume_buffers(v, 0);
+    cudaDeviceSynchronize();
+    delete v;
+    return PVR_OK;
+}
+
+int pvr_volume_release(pvr_volume *v, void *stream) {
+    if (!v) return PVR_OK;
+    pvr::free_volume_buffers(v, (cudaStream_t)stream);
     delete v;
     return PVR_OK;
 }
@@ -297,9 +343,15 @@ int pvr_lut_update(pvr_lut *l, const float *rgba, int size) {
         const bool clear = e[3] == 0.0f && std::isfinite(e[0]) && std::isfinite(e[1]) && std::isfinite(e[2]);
         prefix[i + 1] = prefix[i] + (clear ? 0 : 1);
     }
-    // synchronous copies: ordered after every earlier launch on the legacy stream
-    PVR_CUDA(cudaMemcpy(l->d_lut, rgba, (size_t)size * sizeof(float4), cudaMemcpyHostToDevice));
-    PVR_CUDA(cudaMemcpy(l->d_prefix, prefix.data(), (size_t)(size + 1) * sizeof(int), cudaMemcpyHostToDevice));
+    // copies on a non-blocking stream of this thread: they neither wait for
+    // nor hold up renders on other streams (the caller guarantees that no
+    // queued batch still reads this LUT)
+    thread_local cudaStream_t copy_stream = nullptr;
+    if (!copy_stream) PVR_CUDA(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking));
+    PVR_CUDA(cudaMemcpyAsync(l->d_lut, rgba, (size_t)size * sizeof(float4), cudaMemcpyHostToDevice, copy_stream));
+    PVR_CUDA(cudaMemcpyAsync(l->d_prefix, prefix.data(), (size_t)(size + 1) * sizeof(int),
+                             cudaMemcpyHostToDevice, copy_stream));
+    PVR_CUDA(cudaStreamSynchronize(copy_stream));
     l->size = size;
     l->has_clear = prefix[size] < size;
     return PVR_OK;

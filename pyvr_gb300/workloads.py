@@ -173,3 +173,108 @@ def config_batching(n: int = 64, max_dim: int = 384, resolutions=(128, 256, 512,
                            camera=cam, light=Light.directional([1, -1, 0], 0.2, 0.8), ctf=ctf, otf=otf,
                            config=RenderConfig.balanced(), width=res, height=res))
     return scenes
+
+
+# ---------------------------------------------------------------------------
+# Serving workload
+# ---------------------------------------------------------------------------
+
+def value_noise_device(n: int, seed: int) -> np.ndarray:
+    """value_noise((n, n, n), seed) by the same definition (lattices from
+    default_rng(seed), align-corners trilinear upsampling, weights 0.5^k,
+    min-max normalisation), upsampled on the GPU for speed; float rounding may
+    differ from value_noise in the last bits."""
+    import torch
+    import torch.nn.functional as F
+    rng = np.random.default_rng(seed)
+    acc = torch.zeros((n, n, n), dtype=torch.float32, device="cuda")
+    for k, lat in enumerate((8, 16, 32, 64)):
+        v = torch.from_numpy(rng.random((lat, lat, lat), dtype=np.float32)).cuda()
+        up = F.interpolate(v[None, None], size=(n, n, n), mode="trilinear", align_corners=True)[0, 0]
+        acc += (0.5 ** k) * up
+    lo, hi = acc.min(), acc.max()
+    return ((acc - lo) / (hi - lo)).cpu().numpy()
+
+
+class ServingWorkload:
+    """Seeded serving scenario: a catalog of resident volumes (cubic, extents
+    log-uniform in [min_dim, max_dim], uint8 or float16 value noise, normals
+    computed on the device), per-volume camera/TF sessions, and Poisson
+    request streams with the mix 70% orbit re-renders (azimuth/elevation
+    deltas ~N(0, 0.05) rad, 512^2), 20% TF edits (1-3 opacity points moved by
+    ~N(0, 0.05), then a 512^2 render), 5% high-quality 1024^2 captures, 5%
+    new-volume loads (a volume not resident, uploaded and laid out, then
+    rendered at 512^2)."""
+
+    def __init__(self, n_volumes: int = 32, n_extra: int = 16, min_dim: int = 128,
+                 max_dim: int = 512, seed: int = 0, res: int = 512, capture_res: int = 1024,
+                 generator=None):
+        gen = generator or value_noise_device
+        self.res, self.capture_res = res, capture_res
+        self.light = Light.directional([1, -1, 0], 0.2, 0.8)
+        self.volumes = []  # (Volume, value_scale)
+        rng = np.random.default_rng(seed)
+        for i in range(n_volumes + n_extra):
+            n = int(round(np.exp(rng.uniform(np.log(min_dim), np.log(max_dim)))))
+            dtype = "u8" if rng.random() < 0.5 else "f16"
+            data = to_storage(gen(n, 5000 + i), dtype)
+            vol = Volume(data=data, min_bounds=np.array([-1.0, -1.0, -1.0], np.float32),
+                         max_bounds=np.array([1.0, 1.0, 1.0], np.float32))
+            self.volumes.append((vol, 1.0 / 255.0 if dtype == "u8" else 1.0))
+        self.n_catalog = n_volumes
+        self.catalog = list(range(n_volumes))  # catalog slot -> volume index
+        self.sessions = []
+        for i in range(n_volumes + n_extra):
+            srng = np.random.default_rng(9000 + i)
+            self.sessions.append({
+                "az": float(srng.uniform(-np.pi, np.pi)), "el": float(srng.uniform(-0.8, 0.8)),
+                "dist": float(srng.uniform(2.5, 4.0)),
+                "otf": [(float(x), float(y)) for x, y in zip(np.sort(srng.random(6)),
+                                                            srng.uniform(0.0, 0.3, 6))],
+                "ctf": standin_colormap(int(srng.integers(0, N_STANDIN_COLORMAPS)))})
+        self._next_extra = n_volumes
+
+    def camera(self, vidx: int) -> Camera:
+        s = self.sessions[vidx]
+        return Camera.from_spherical(target=np.zeros(3, np.float32), azimuth=s["az"],
+                                     elevation=s["el"], roll=0.0, distance=s["dist"])
+
+    def requests(self, rate: float, duration: float, seed: int):
+        """[(arrival offset s, kwargs of RenderRequest)] for a Poisson stream."""
+        rng = np.random.default_rng(seed)
+        t, out = 0.0, []
+        while True:
+            t += rng.exponential(1.0 / rate)
+            if t >= duration:
+                return out
+            u = rng.random()
+            slot = int(rng.integers(0, self.n_catalog))
+            kind, w, cfg = "render", self.res, RenderConfig.balanced()
+            if u < 0.70:
+                tag = "orbit"
+            elif u < 0.90:
+                tag = "tf_edit"
+            elif u < 0.95:
+                tag, w, cfg = "capture", self.capture_res, RenderConfig.high_quality()
+            else:
+                tag, kind = "load", "load"
+                # a volume that is not in the catalog replaces a catalog slot
+                out_of_catalog = [i for i in range(len(self.volumes)) if i not in self.catalog]
+                self.catalog[slot] = out_of_catalog[int(rng.integers(0, len(out_of_catalog)))]
+            vidx = self.catalog[slot]
+            s = self.sessions[vidx]
+            if tag == "orbit":
+                s["az"] += float(rng.normal(0.0, 0.05))
+                s["el"] = float(np.clip(s["el"] + rng.normal(0.0, 0.05), -1.5, 1.5))
+            elif tag == "tf_edit":
+                pts = list(s["otf"])
+                for k in rng.choice(len(pts), size=int(rng.integers(1, 4)), replace=False):
+                    x, y = pts[k]
+                    pts[k] = (float(np.clip(x + rng.normal(0, 0.05), 0, 1)),
+                              float(np.clip(y + rng.normal(0, 0.05), 0, 1)))
+                s["otf"] = sorted(pts)
+            vol, vs = self.volumes[vidx]
+            out.append((t, dict(kind=kind, volume_id=vidx, camera=self.camera(vidx), light=self.light,
+                                config=cfg, color_tf=s["ctf"],
+                                opacity_tf=OpacityTransferFunction(list(s["otf"])), width=w, height=w,
+                                value_scale=vs, volume=vol, tag=tag)))

@@ -1,0 +1,72 @@
+"""Serving: every result of the continuously batched server equals the same
+request rendered alone (and the CPU oracle), with and without evictions."""
+
+import numpy as np
+import pytest
+
+import oracle
+from pyvr_gb300 import workloads as W
+from pyvr_gb300.renderer import rgba_lut
+from pyvr_gb300.server import RenderRequest, RenderServer, SerialRenderer, latency_stats
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def _workload():
+    return W.ServingWorkload(n_volumes=5, n_extra=3, min_dim=16, max_dim=40, res=48, capture_res=64,
+                             generator=lambda n, s: W.value_noise((n, n, n), s))
+
+
+def _run(budget, n_req=160):
+    wl = _workload()
+    stream = wl.requests(rate=4000.0, duration=1.0, seed=3)[:n_req]
+    server = RenderServer(budget_bytes=budget, max_batch=16, slots=3)
+    serial = SerialRenderer()
+    for slot in range(wl.n_catalog):
+        vol, vs = wl.volumes[slot]
+        server.cache.insert(slot, vol, vs, server._release_after_inflight)
+        serial.cache.insert(slot, vol, vs, serial._free_now)
+    reqs = [RenderRequest(**kw) for _, kw in stream]
+    futs = [server.submit(r) for r in reqs]
+    got = [f.result(timeout=120) for f in futs]
+    want = []
+    for _, kw in stream:
+        req = RenderRequest(**kw)
+        if req.kind == "render" and serial.cache.get(req.volume_id) is None:
+            req.kind = "load"  # the serial cache may have evicted / never seen it
+        want.append(serial.handle(req))
+    stats = dict(batches=server.batches, sizes=list(server.batch_sizes),
+                 evictions=server.cache.evictions, loads=server.cache.loads, lat=latency_stats(reqs))
+    server.close()
+    serial.close()
+    return wl, stream, got, want, stats
+
+
+def test_server_results_equal_results_alone():
+    wl, stream, got, want, stats = _run(budget=40 << 30)
+    assert len(got) == len(want) == len(stream)
+    for g, w in zip(got, want):
+        assert g == w
+    assert max(stats["sizes"]) > 1, stats["sizes"]  # requests were really batched
+    tags = {kw["tag"] for _, kw in stream}
+    assert {"orbit", "tf_edit", "capture", "load"} <= tags
+    # a few results against the CPU oracle
+    for (_, kw), g in list(zip(stream, got))[:6]:
+        vol, vs = wl.volumes[kw["volume_id"]]
+        from pyvr_gb300 import compute_normal_volume, Volume
+        v = Volume(data=vol.data, normals=compute_normal_volume(vol.data), min_bounds=vol.min_bounds,
+                   max_bounds=vol.max_bounds)
+        lut = rgba_lut(kw["color_tf"], kw["opacity_tf"])
+        o8, _, _ = oracle.render(W.frame_inputs(v, kw["camera"], kw["light"], kw["config"], lut,
+                                                kw["width"], kw["height"], vs), want_float=False)
+        assert g == o8.tobytes()
+
+
+def test_server_with_evictions():
+    # room for about two of the small volumes: loads and re-loads evict others
+    wl, stream, got, want, stats = _run(budget=3 << 20, n_req=120)
+    for g, w in zip(got, want):
+        assert g == w
+    assert stats["evictions"] > 0
