@@ -3,22 +3,28 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-Workload ("plain at scale"): a 256^3 value-noise volume (seed 0) stored as
-uint8 (read as UNORM), float16 and float32, each with float32 normals, 16
-orbit cameras (azimuth 2*pi*k/16, elevation pi/6, distance 3), 1024x1024
-RGBA8, RenderConfig.high_quality(), 8 seeded opacity points in [0, 0.3] and
-a stand-in colour map.  One step renders all 48 frames (3 storages x 16
-cameras).  Inputs (volume + normals, 208-256 MiB per storage) exceed the
-129 MB L2.
+Headline ("renders/s & p50/p99 ms: batched server vs per-frame CUDA"):
+the serving workload -- a catalog of 32 HBM-resident volumes (cubic,
+extents log-uniform in 128..512, uint8 or float16 value noise, normals
+computed on the GPU) under a 40 GB budget with LRU eviction, and a seeded
+Poisson request stream mixing 70% orbit re-renders (512^2, balanced), 20% TF
+edits (512^2), 5% high-quality 1024^2 captures and 5% new-volume loads.
+For the continuously batching server and for the serial per-frame renderer
+(same resident volumes, one request at a time), an untimed sweep of offered
+rates (doubling from 400 req/s) finds the highest rate served with p99
+latency <= 20 ms; then K timed steps -- one second of the request stream
+each -- run at that rate.  value = requests completed per second by the
+server (arrival -> RGBA8 bytes in host memory: the whole path is end to end);
+the per-frame renderer's rate, the ratio and p50/p99 of both (also at the
+nominal 400 req/s) are reported beside it.  The roofline is the batch march
+kernel's (event-timed launches inside the timed steps; bytes = 8 voxel texels
+in the stored type + 8 float32x3 normal texels per shaded in-box sample).
 
-value   : frames/s with the volume resident in HBM, device-timed (CUDA events)
-e2e     : frames/s through the public API (set_camera + render() -> bytes,
-          read back to host memory every frame)
-roofline: the march kernel's algorithmic bytes (8 texels of the stored volume
-          + 8 float32x3 normal texels per in-box sample) per launch over its
-          event-timed duration, against the measured HBM copy bandwidth.
+Nested "plain" section: the per-frame renderer on 256^3 value noise in
+u8/f16/f32, 16 orbit cameras, 1024^2, high_quality (one step = 48 frames).
+
 --impl reference: the CPU restatement of the reference shader (the oracle,
-          OpenMP over all host cores) on bounded row bands of the same frames.
+all host cores) serving the same request mix, on bounded row bands.
 """
 
 import argparse
@@ -38,6 +44,8 @@ BYTES_PER_SAMPLE = {"u8": 8 * 1 + 8 * 12, "f16": 8 * 2 + 8 * 12, "f32": 8 * 4 + 
 DTYPES = ("u8", "f16", "f32")
 RES = 1024
 N_VOL = 256
+NOMINAL_RATE = 400.0
+P99_MS = 20.0
 
 
 def parse_args():
@@ -46,8 +54,13 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--cpu-rows", type=int, default=256, help="rows per CPU-baseline sample band")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="oracle seconds of the CPU baseline")
+    ap.add_argument("--probe-s", type=float, default=2.0, help="seconds per rate probe")
+    ap.add_argument("--refine", type=int, default=3, help="bisection probes after the doubling sweep")
+    ap.add_argument("--serving-volumes", type=int, default=32)
+    ap.add_argument("--serving-max-dim", type=int, default=512)
     # smaller cases for profiling captures
+    ap.add_argument("--only", choices=["all", "plain", "serving"], default="all")
     ap.add_argument("--storages", default=",".join(DTYPES))
     ap.add_argument("--cameras", type=int, default=16)
     ap.add_argument("--skip-cpu", action="store_true")
@@ -126,90 +139,143 @@ def gpu_index(local_rank):
     return local_rank
 
 
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle (a checker here, timed; never the product path)
+# ---------------------------------------------------------------------------
+
+def cpu_serving_sample(workload, target_s, seed, max_dim=256, max_req=400):
+    """Whole-frame oracle renders of render requests from the serving mix, in
+    arrival order, until target_s seconds of oracle time (at least one).
+    Catalog volumes up to max_dim^3 only, so that the host normals stay small.
+    Returns (seconds, requests, in-box samples, threads)."""
+    import oracle
+    from pyvr_gb300 import Volume, compute_normal_volume
+    from pyvr_gb300 import workloads as W
+    from pyvr_gb300.renderer import rgba_lut
+    oracle.build()
+    normals = {}  # id(data) -> (data, normals): the data reference keeps the id unique
+    total_t, total_n, done = 0.0, 0, 0
+    for _, kw in workload.requests(NOMINAL_RATE, 30.0, seed):
+        if kw["kind"] != "render" or kw["volume"].data.shape[0] > max_dim:
+            continue
+        v = kw["volume"]
+        if id(v.data) not in normals:
+            normals[id(v.data)] = (v.data, compute_normal_volume(v.data))
+        vol = Volume(data=v.data, normals=normals[id(v.data)][1], min_bounds=v.min_bounds,
+                     max_bounds=v.max_bounds)
+        lut = rgba_lut(kw["color_tf"], kw["opacity_tf"])
+        s = W.frame_inputs(vol, kw["camera"], kw["light"], kw["config"], lut, kw["width"], kw["height"],
+                           kw["value_scale"], batch_camera=True)
+        t = time.perf_counter()
+        _, _, n = oracle.render(s, want_float=False)
+        total_t += time.perf_counter() - t
+        total_n += n
+        done += 1
+        if total_t >= target_s or done >= max_req:
+            break
+    return total_t, done, total_n, oracle.max_threads()
+
+
+# ---------------------------------------------------------------------------
+# Serving (headline)
+# ---------------------------------------------------------------------------
+
+def pin_host_volumes(workload, torch):
+    """Page-lock the host copies of the volumes (the data a client hands in)."""
+    cudart = torch.cuda.cudart()
+    for vol, _ in workload.volumes:
+        a = vol.data
+        cudart.cudaHostRegister(a.ctypes.data, a.nbytes, 0)
+
+
+def serving_section(args, torch):
+    from pyvr_gb300 import workloads as W
+    from pyvr_gb300.server import RenderServer, SerialRenderer, drive, latency_stats, sustained_rate
+    t_setup = time.perf_counter()
+    wl = W.ServingWorkload(n_volumes=args.serving_volumes, n_extra=16, min_dim=128,
+                           max_dim=args.serving_max_dim, seed=0)
+    pin_host_volumes(wl, torch)
+    server = RenderServer(budget_bytes=40 << 30, max_batch=64, slots=3, instrument=True)
+    serial = SerialRenderer(budget_bytes=40 << 30)
+    for slot in range(wl.n_catalog):
+        vol, vs = wl.volumes[slot]
+        server.cache.insert(slot, vol, vs, server._release_after_inflight)
+        serial.cache.insert(slot, vol, vs, serial._free_now)
+    torch.cuda.synchronize()
+    setup_s = time.perf_counter() - t_setup
+    # warm-up: W untimed one-second segments at the nominal rate, each impl
+    for w in range(args.warmup):
+        drive(server, wl.requests(NOMINAL_RATE, 1.0, 100 + w))
+        drive(serial, wl.requests(NOMINAL_RATE, 1.0, 150 + w))
+    # latency at the nominal rate, both (reported, untimed)
+    nom = {}
+    for name, impl in (("server", server), ("serial", serial)):
+        reqs, el = drive(impl, wl.requests(NOMINAL_RATE, 3.0, 200))
+        st = latency_stats(reqs)
+        st["completed_per_s"] = len(reqs) / el
+        nom[name] = st
+    # untimed sweep: highest rate with p99 <= 20 ms
+    rates = [NOMINAL_RATE * (2 ** k) for k in range(7)]
+    r_server, probes_server = sustained_rate(server, wl, rates, args.probe_s, 300, refine=args.refine)
+    r_serial, probes_serial = sustained_rate(serial, wl, rates, args.probe_s, 400, refine=args.refine)
+    r_server = r_server or NOMINAL_RATE
+    r_serial = r_serial or NOMINAL_RATE
+    # timed: K one-second steps at the sustained rate, server then serial
+    clocks = ClockSampler(gpu_index(dist_env()[2]))
+    clocks.start()
+    server.kernel_records.clear()
+    lut_misses0 = server.luts.misses
+    torch.cuda.synchronize()
+    srv_reqs, srv_el = drive(server, wl.requests(r_server, float(args.steps), 500))
+    torch.cuda.synchronize()
+    ser_reqs, ser_el = drive(serial, wl.requests(r_serial, float(args.steps), 600))
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    records = list(server.kernel_records)
+    # roofline of the batch march kernel over the timed steps
+    k_ms = sum(r[0] for r in records)
+    k_bytes = sum(sh * BYTES_PER_SAMPLE["u8" if vs != 1.0 else "f16"]
+                  for r in records for (_, _, vs, sh) in r[3])
+    peak, peak_kind = measured_peaks()
+    achieved = k_bytes / (k_ms / 1000.0) / 1e9 if k_ms else 0.0
+    d2h = sum(r.width * r.height * 4 for r in srv_reqs)
+    # uploads: new volumes, and tables of transfer functions not yet resident
+    # (entries float4 + skip prefix int32)
+    h2d = (sum(r.volume.data.nbytes for r in srv_reqs if r.tag == "load")
+           + (server.luts.misses - lut_misses0) * (256 * 16 + 257 * 4))
+    inbox = sum(r[1] for r in records)
+    out = dict(value=len(srv_reqs) / srv_el, serial_value=len(ser_reqs) / ser_el,
+               server=latency_stats(srv_reqs), serial=latency_stats(ser_reqs), nominal=nom,
+               rate_server=r_server, rate_serial=r_serial, probes_server=probes_server,
+               probes_serial=probes_serial, batches=len(records),
+               mean_batch=(statistics.mean(len(r[3]) for r in records) if records else 0),
+               kernel_ms=k_ms, inbox_samples=inbox, shaded_samples=sum(r[2] for r in records),
+               mean_inbox_per_request=inbox / max(1, sum(len(r[3]) for r in records)),
+               roofline={"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                         "kernel": "march_batch_kernel",
+                         "note": "batches in flight on different streams may overlap; summed launch "
+                                 "times make this a lower bound"},
+               clocks=clk, h2d=h2d / args.steps, d2h=d2h / args.steps, setup_s=setup_s,
+               loads=server.cache.loads, evictions=server.cache.evictions,
+               lut_hits=server.luts.hits, lut_misses=server.luts.misses, workload=wl)
+    server.close()
+    serial.close()
+    return out
+
+
+# ---------------------------------------------------------------------------
+# Plain per-frame renderer (nested section)
+# ---------------------------------------------------------------------------
+
 def make_scenes(storages=DTYPES):
     from pyvr_gb300 import workloads as W
     noise = W.config_scale_volume(N_VOL)
     return {dt: W.config_scale(dt, n=N_VOL, res=RES, noise=noise) for dt in storages}
 
 
-def cpu_sample(scenes, rows, nthreads=0, cams=(0, 4, 8, 12)):
-    """Time the oracle on a band of rows of the given frames; returns
-    (seconds, in-box samples, threads)."""
-    import oracle
-    from pyvr_gb300 import workloads as W
-    from pyvr_gb300.renderer import rgba_lut
-    oracle.build()
-    r0 = RES // 2 - rows // 2
-    total_t, total_n = 0.0, 0
-    for dt, c in scenes.items():
-        lut = rgba_lut(c["ctf"], c["otf"])
-        for k in cams:
-            s = W.frame_inputs(c["volume"], c["cameras"][k], c["light"], c["config"], lut, RES,
-                               RES, c["value_scale"])
-            t = time.perf_counter()
-            _, _, n = oracle.render(s, rows=(r0, r0 + rows), want_float=False, nthreads=nthreads)
-            total_t += time.perf_counter() - t
-            total_n += n
-    return total_t, total_n, (nthreads or oracle.max_threads())
-
-
-def run_reference(args):
-    rank, world, _ = dist_env()
-    if rank != 0:
-        return
-    scenes = make_scenes()
-    # samples of each full frame, for extrapolating band timings to frames/s:
-    # the band's share of the frame's samples is estimated from the oracle
-    # itself on a coarse (every 8th row) pass
-    import oracle
-    from pyvr_gb300 import workloads as W
-    from pyvr_gb300.renderer import rgba_lut
-    frame_samples = {}
-    for dt, c in scenes.items():
-        lut = rgba_lut(c["ctf"], c["otf"])
-        s = W.frame_inputs(c["volume"], c["cameras"][3], c["light"], c["config"], lut, RES, RES,
-                           c["value_scale"])
-        tot = 0
-        for r in range(0, RES, 16):
-            tot += oracle.render(s, rows=(r, r + 1), want_float=False)[2]
-        frame_samples[dt] = tot * 16
-    times, rates = [], []
-    for i in range(args.warmup + args.steps):
-        t, n, threads = cpu_sample(scenes, args.cpu_rows)
-        if i >= args.warmup:
-            times.append(t)
-            # frames/s: samples/s over the mean samples of one full frame
-            rates.append(n / t / statistics.mean(frame_samples.values()))
-    value = statistics.mean(rates)
-    line = {"impl": "reference", "metric": "plain per-frame renders/s (256^3, 1024^2, high_quality)",
-            "value": value, "unit": "renders/s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1000 * statistics.mean(times),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": config_dict(args),
-            "cpu_baseline": {"kind": "port", "cores": threads, "value": value, "unit": "renders/s",
-                             "sample": f"rows {RES // 2 - args.cpu_rows // 2}..+{args.cpu_rows} of cameras 0,4,8,12, "
-                                       f"each of u8/f16/f32, per step; frames/s = samples/s / samples per frame"},
-            "e2e": {"value": value, "unit": "renders/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line))
-
-
-def config_dict(args):
-    storages = args.storages.split(",")
-    return {"workload": "plain_at_scale", "volume": f"{N_VOL}^3 value noise seed 0",
-            "storages": storages, "cameras": args.cameras, "resolution": f"{RES}x{RES}",
-            "render_config": "high_quality", "frames_per_step": args.cameras * len(storages),
-            "parallelism": f"replicas x{args.gpus}", "l2": "inputs larger than L2 (208-256 MiB per storage)"}
-
-
-def run_ours(args):
-    import torch
-    rank, world, local_rank = dist_env()
-    torch.cuda.set_device(local_rank)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+def plain_section(args, torch):
     from pyvr_gb300 import VolumeRenderer, _native
-
     scenes = make_scenes(tuple(args.storages.split(",")))
     lib = _native.load()
     rend = {}
@@ -222,13 +288,8 @@ def run_ours(args):
     # an explicit stream: handle 0 (the legacy default stream) would mean
     # "the renderer's own stream" to the C ABI
     stream = torch.cuda.Stream()
-    torch.cuda.set_stream(stream)
     sptr = ctypes.c_void_p(stream.cuda_stream)
-    assert sptr.value
     out = torch.empty(RES * RES * 4, dtype=torch.uint8, device="cuda")
-
-    # per-frame in-box and shaded sample counts (deterministic), from one
-    # counted pass; the roofline counts the bytes of shaded samples only
     samples, shaded = {}, {}
     for dt, r in rend.items():
         for k, cam in enumerate(cams):
@@ -248,17 +309,9 @@ def run_ours(args):
                 if events is not None:
                     events[-1][3].record(stream)
 
-    def barrier():
-        torch.cuda.synchronize()
-        if world > 1:
-            torch.distributed.barrier()
-            torch.cuda.synchronize()
-
     for _ in range(args.warmup):
         device_step()
-    clocks = ClockSampler(gpu_index(local_rank))
-    clocks.start()
-    barrier()
+    torch.cuda.synchronize()
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
     events = []
@@ -266,80 +319,148 @@ def run_ours(args):
     for _ in range(args.steps):
         device_step(events)
     t1.record(stream)
-    barrier()
-    clk = clocks.stop()
+    torch.cuda.synchronize()
     elapsed = t0.elapsed_time(t1) / 1000.0
     launch_ms = [(dt, k, a.elapsed_time(b)) for dt, k, a, b in events]
-
-    # end to end through the public API, host bytes back every frame
-    e2e_elapsed = float("nan")
+    e2e = None
     if not args.skip_e2e:
         for dt, r in rend.items():
             for cam in cams:
                 r.set_camera(cam)
                 r.render()
-        barrier()
+        torch.cuda.synchronize()
         te = time.perf_counter()
         for _ in range(args.steps):
             for dt, r in rend.items():
                 for cam in cams:
                     r.set_camera(cam)
                     r.render()
-        barrier()
-        e2e_elapsed = time.perf_counter() - te
-
-    frames_per_step = len(rend) * len(cams)
-    if world > 1:
-        t = torch.tensor([elapsed, e2e_elapsed], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        elapsed, e2e_elapsed = t.tolist()
-    value = world * args.steps * frames_per_step / elapsed
-    e2e_value = (None if args.skip_e2e else
-                 world * args.steps * frames_per_step / e2e_elapsed)
-
-    # roofline of the march kernel (algorithmic bytes over event-timed launches)
+        torch.cuda.synchronize()
+        e2e = args.steps * len(rend) * len(cams) / (time.perf_counter() - te)
+    frames = args.steps * len(rend) * len(cams)
     tot_bytes = sum(shaded[(dt, k)] * BYTES_PER_SAMPLE[dt] for dt, k, _ in launch_ms)
     tot_s = sum(ms for _, _, ms in launch_ms) / 1000.0
-    achieved = tot_bytes / tot_s / 1e9
     peak, peak_kind = measured_peaks()
-    tot_samples = sum(samples[(dt, k)] for dt, k, _ in launch_ms)
     per_dtype = {}
     for dt in rend:
         ms = [m for d, _, m in launch_ms if d == dt]
         by = sum(shaded[(d, k)] * BYTES_PER_SAMPLE[d] for d, k, _ in launch_ms if d == dt)
-        per_dtype[dt] = {"avg_launch_ms": statistics.mean(ms),
-                         "gbs": by / (sum(ms) / 1000.0) / 1e9,
-                         "samples_per_frame": statistics.mean(samples[(dt, k)] for k in range(len(cams))),
-                         "shaded_per_frame": statistics.mean(shaded[(dt, k)] for k in range(len(cams)))}
-
-    cpu = None
-    if rank == 0 and not args.skip_cpu:
-        ct, cn, threads = cpu_sample(scenes, args.cpu_rows)
-        mean_frame = statistics.mean(samples.values())
-        cpu = {"value": cn / ct / mean_frame, "unit": "renders/s", "cores": threads, "kind": "port",
-               "sample": f"oracle on rows {RES // 2 - args.cpu_rows // 2}..+{args.cpu_rows} of cameras 0,4,8,12 "
-                         f"for u8/f16/f32 ({cn} samples in {ct:.1f} s); renders/s = samples/s / "
-                         f"mean in-box samples per frame",
-               "samples_per_s": cn / ct}
+        per_dtype[dt] = {"avg_launch_ms": statistics.mean(ms), "gbs": by / (sum(ms) / 1000.0) / 1e9,
+                         "samples_per_frame": statistics.mean(samples[(dt, k)] for k in range(len(cams)))}
     for r in rend.values():
         r.close()
+    return {"frames_per_s": frames / elapsed, "e2e_frames_per_s": e2e,
+            "ms_per_frame": 1000.0 * elapsed / frames,
+            "samples_per_s": sum(samples[(dt, k)] for dt, k, _ in launch_ms) / elapsed,
+            "roofline": {"bound": "hbm", "achieved": tot_bytes / tot_s / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": tot_bytes / tot_s / 1e9 / peak, "peak_kind": peak_kind,
+                         "kernel": "march_single_kernel", "per_storage": per_dtype},
+            "gpu_launches": len(launch_ms),
+            "config": {"volume": f"{N_VOL}^3 value noise seed 0", "storages": list(rend),
+                       "cameras": len(cams), "resolution": f"{RES}x{RES}", "render_config": "high_quality",
+                       "frames_per_step": len(rend) * len(cams),
+                       "l2": "inputs larger than L2 (208-256 MiB per storage)"}}
+
+
+# ---------------------------------------------------------------------------
+
+def serving_config(args):
+    return {"workload": "serving: 32 resident volumes 128^3-512^3 u8/f16 (value noise, device normals), "
+                        "Poisson stream 70% orbit 512^2 / 20% TF edit 512^2 / 5% 1024^2 high_quality "
+                        "capture / 5% new-volume load, 40 GB budget, LRU",
+            "step": "one second of the request stream at the sustained rate",
+            "sustained": f"highest offered rate with p99 <= {P99_MS:.0f} ms and completions >= 0.9x "
+                         f"offered, found by an untimed sweep (doubling from {NOMINAL_RATE:.0f} req/s, "
+                         f"then {args.refine} bisection probes)",
+            "parallelism": f"replicas x{args.gpus}",
+            "l2": "resident volumes (~25 GB) far exceed L2"}
+
+
+def run_ours(args):
+    import torch
+    rank, world, local_rank = dist_env()
+    torch.cuda.set_device(local_rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    plain = plain_section(args, torch) if args.only in ("all", "plain") else None
+    if args.only == "plain":
+        if rank == 0:
+            print(json.dumps({"plain": plain}))
+        return
+    s = serving_section(args, torch)
+    value, serial_value = s["value"], s["serial_value"]
+    if world > 1:
+        # replicas: each rank serves its own stream; the job's rate is the sum
+        t = torch.tensor([value, serial_value], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t)
+        value, serial_value = t.tolist()
+    cpu = None
+    if rank == 0 and not args.skip_cpu:
+        ct, nreq, cn, threads = cpu_serving_sample(s["workload"], args.cpu_seconds, 700)
+        cpu = {"value": nreq / ct, "unit": "renders/s", "cores": threads, "kind": "port",
+               "sample": f"oracle, whole frames of the first {nreq} render requests of a stream of the "
+                         f"mix (catalog volumes <= 256^3) in {ct:.1f} s on {threads} threads",
+               "samples_per_s": cn / ct}
     if rank == 0:
-        line = {"metric": "plain per-frame renders/s (256^3, 1024^2, high_quality)",
+        srv = s["server"]
+        line = {"metric": "renders/s (batched server, mixed request stream, p99 <= 20 ms)",
                 "value": value, "unit": "renders/s", "n_gpus": world, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": 1000 * elapsed / args.steps,
+                "warmup": args.warmup, "ms_per_step": 1000.0,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-                "data": "synthetic", "config": config_dict(args),
-                "samples_per_s": world * args.steps * (tot_samples / args.steps) / elapsed,
-                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                             "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
-                             "kernel": "march_kernel", "per_storage": per_dtype},
-                "cpu_baseline": cpu, "clocks": clk,
-                "e2e": {"value": e2e_value, "unit": "renders/s", "h2d_bytes_per_step": 0,
-                        "d2h_bytes_per_step": frames_per_step * RES * RES * 4},
-                "gpu_launches": len(launch_ms)}
+                "data": "synthetic", "config": serving_config(args),
+                "p50_ms": srv.get("p50_ms"), "p99_ms": srv.get("p99_ms"),
+                "serial_per_frame": {"renders_per_s": serial_value, "p50_ms": s["serial"].get("p50_ms"),
+                                     "p99_ms": s["serial"].get("p99_ms"), "sustained_offered": s["rate_serial"]},
+                "server_over_serial": value / serial_value if serial_value else None,
+                "sustained_offered": s["rate_server"],
+                "nominal_400": s["nominal"],
+                "probes": {"server": s["probes_server"], "serial": s["probes_serial"]},
+                "batching": {"batches": s["batches"], "mean_jobs_per_batch": s["mean_batch"],
+                             "loads": s["loads"], "evictions": s["evictions"]},
+                "samples": {"inbox": s["inbox_samples"], "shaded": s["shaded_samples"],
+                            "mean_inbox_per_request": s["mean_inbox_per_request"]},
+                "roofline": s["roofline"], "cpu_baseline": cpu, "clocks": s["clocks"],
+                "e2e": {"value": value, "unit": "renders/s", "h2d_bytes_per_step": s["h2d"],
+                        "d2h_bytes_per_step": s["d2h"]},
+                "gpu_launches": s["batches"],
+                "plain": plain}
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_reference(args):
+    """The oracle (CPU, all host cores) serving the same request mix."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from pyvr_gb300 import workloads as W
+    wl = W.ServingWorkload(n_volumes=args.serving_volumes, n_extra=16, min_dim=128,
+                           max_dim=args.serving_max_dim, seed=0,
+                           generator=lambda n, s: W.value_noise((n, n, n), s))
+    times, reqs, samples = [], 0, 0
+    threads = 1
+    per_step = max(1.0, args.cpu_seconds / max(1, args.steps))
+    for i in range(args.warmup + args.steps):
+        t, nreq, n, threads = cpu_serving_sample(wl, per_step if i >= args.warmup else 0.0, 800 + i)
+        if i >= args.warmup:
+            times.append(t)
+            reqs += nreq
+            samples += n
+    value = reqs / sum(times) if times else 0.0
+    line = {"impl": "reference", "metric": "renders/s (batched server, mixed request stream, p99 <= 20 ms)",
+            "value": value, "unit": "renders/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * statistics.mean(times), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": serving_config(args),
+            "cpu_baseline": {"kind": "port", "cores": threads, "value": value, "unit": "renders/s",
+                             "sample": f"per step: whole frames of render requests of the mix (catalog "
+                                       f"volumes <= 256^3) for >= {per_step:.1f} s of oracle time on "
+                                       f"{threads} threads; {reqs} requests in {sum(times):.1f} s",
+                             "samples_per_s": samples / sum(times) if times else 0.0},
+            "e2e": {"value": value, "unit": "renders/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
 
 
 def main():

@@ -211,6 +211,23 @@ int pvr_batch_render(pvr_batch *b, const pvr_job *jobs, int n, void *stream);
 /* Wait for every batch queued on this launcher. */
 int pvr_batch_synchronize(pvr_batch *b);
 
+/* Orbit camera setup on the host in double precision: Camera.from_spherical
+ * + get_camera_vectors / get_view_matrix / get_projection_matrix(aspect)
+ * (pyvr/camera/control.py:238-351, pyvr/camera/camera.py:292-369), giving the
+ * float32 view, projection and position pvr_set_camera / pvr_job take.
+ * Agrees with the reference's float32 arrays to float32 rounding.  Fails
+ * with PVR_ERR_VALUE (nothing written) when the rotated up vector is parallel
+ * to the view direction, where the reference's basis is rounding noise. */
+int pvr_camera_spherical(const float target[3], double azimuth, double elevation, double roll,
+                         double distance, const float init_pos[3], const float init_up[3], double fov,
+                         double near_plane, double far_plane, double aspect, float view_out[16],
+                         float proj_out[16], float pos_out[3]);
+
+/* Page-locked host memory mapped for the device (a job's d_rgba8 may point
+ * at device_ptr: the kernel then writes the image straight to host memory). */
+int pvr_host_buffer_create(long long bytes, void **host_ptr, void **device_ptr);
+int pvr_host_buffer_free(void *host_ptr);
+
 #ifdef __cplusplus
 }
 #endif

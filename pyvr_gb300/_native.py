@@ -126,6 +126,11 @@ SIGNATURES = {
     "pvr_batch_get_tuning": (_I, [_VP, _VP]),
     "pvr_batch_render": (_I, [_VP, _VP, _I, _VP]),
     "pvr_batch_synchronize": (_I, [_VP]),
+    "pvr_camera_spherical": (_I, [_FP, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                  _FP, _FP, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                  ctypes.c_double, _FP, _FP, _FP]),
+    "pvr_host_buffer_create": (_I, [_LL, ctypes.POINTER(_VP), ctypes.POINTER(_VP)]),
+    "pvr_host_buffer_free": (_I, [_VP]),
 }
 
 PVR_NORMALS_NONE, PVR_NORMALS_GIVEN, PVR_NORMALS_DEVICE = 0, 1, 2

@@ -17,7 +17,7 @@ import numpy as np
 
 from . import _native
 from ._native import check
-from .renderer import camera_uniforms, rgba_lut, volume_storage
+from .renderer import rgba_lut, volume_storage
 
 
 def _lib():
@@ -142,27 +142,81 @@ def _ptr(x) -> Optional[int]:
     return int(x.data_ptr())
 
 
+_F3 = ctypes.c_float * 3
+
+
+def _f3(v) -> "ctypes.Array":
+    return _F3(float(v[0]), float(v[1]), float(v[2]))
+
+
+def fill_camera(camera, width: int, height: int, view, proj, pos) -> None:
+    """Orbit camera -> float32 view / projection / position, computed natively
+    in double precision (``pvr_camera_spherical``) into the ctypes arrays
+    ``view`` (16), ``proj`` (16) and ``pos`` (3).  Same construction as
+    ``Camera.get_view_matrix`` / ``get_projection_matrix`` /
+    ``get_camera_vectors`` (pyvr/camera/camera.py:292-369,
+    pyvr/camera/control.py:238-351), agreeing with them to float32 rounding,
+    at a few microseconds instead of a few hundred.  A camera whose up vector
+    ends parallel to the view direction has a basis made of rounding noise;
+    that case takes the ``Camera`` methods' matrices."""
+    rc = _lib().pvr_camera_spherical(
+        _f3(camera.target), float(camera.azimuth), float(camera.elevation), float(camera.roll),
+        float(camera.distance), _f3(camera.init_pos), _f3(camera.init_up), float(camera.fov),
+        float(camera.near_plane), float(camera.far_plane), float(width) / float(height),
+        view, proj, pos)
+    if rc == _native.PVR_ERR_VALUE and b"parallel" in _lib().pvr_last_error():
+        from .renderer import camera_uniforms
+        v, p, c = camera_uniforms(camera, width, height)
+        for dst, src in ((view, v), (proj, p), (pos, c)):
+            for i, x in enumerate(src.ravel().tolist()):
+                dst[i] = x
+        return
+    check(rc)
+
+
+def job_camera_uniforms(camera, width: int, height: int):
+    """(view, proj, position) float32 numpy arrays as the batch path computes
+    them (``fill_camera``)."""
+    view = np.zeros((4, 4), np.float32)
+    proj = np.zeros((4, 4), np.float32)
+    pos = np.zeros(3, np.float32)
+    fp = ctypes.POINTER(ctypes.c_float)
+    fill_camera(camera, width, height, view.ctypes.data_as(fp), proj.ctypes.data_as(fp),
+                pos.ctypes.data_as(fp))
+    return view, proj, pos
+
+
+def fill_job(j: _native.PvrJob, volume: int, lut: int, camera, light, config, width: int,
+             height: int, d_rgba8: Optional[int] = None, d_rgba32f: Optional[int] = None,
+             d_counters: Optional[int] = None) -> None:
+    """Fill a ``pvr_job`` in place from raw handles / device addresses (ints)
+    and camera / light / config objects (pyvr's or this package's)."""
+    fill_camera(camera, width, height, j.view, j.proj, j.camera_pos)
+    j.volume = volume
+    j.lut = lut
+    j.width = width
+    j.height = height
+    lp, lt = light.position, light.target
+    j.light_pos[0], j.light_pos[1], j.light_pos[2] = float(lp[0]), float(lp[1]), float(lp[2])
+    j.light_target[0], j.light_target[1], j.light_target[2] = float(lt[0]), float(lt[1]), float(lt[2])
+    j.ambient = float(light.ambient_intensity)
+    j.diffuse = float(light.diffuse_intensity)
+    j.step_size = float(config.step_size)
+    j.reference_step_size = float(config.reference_step_size)
+    j.max_steps = int(config.max_steps)
+    j.d_rgba8 = d_rgba8
+    j.d_rgba32f = d_rgba32f
+    j.d_counters = d_counters
+
+
 def make_job_struct(job: RenderJob, out: Optional[_native.PvrJob] = None) -> _native.PvrJob:
+    """A ``pvr_job`` for ``job``.  The camera goes through ``fill_camera``
+    (native double-precision setup), so an oracle scene for a batch render is
+    built from ``job_camera_uniforms``."""
     j = out if out is not None else _native.PvrJob()
-    view, proj, pos = camera_uniforms(job.camera, job.width, job.height)
-    j.volume = job.volume.handle.value
-    j.lut = job.lut.handle.value
-    j.width, j.height = int(job.width), int(job.height)
-    j.view[:] = view.ravel().tolist()
-    j.proj[:] = proj.ravel().tolist()
-    j.camera_pos[:] = pos.tolist()
-    lp = np.asarray(job.light.position, np.float32)
-    lt = np.asarray(job.light.target, np.float32)
-    j.light_pos[:] = lp.tolist()
-    j.light_target[:] = lt.tolist()
-    j.ambient = float(job.light.ambient_intensity)
-    j.diffuse = float(job.light.diffuse_intensity)
-    j.step_size = float(job.config.step_size)
-    j.reference_step_size = float(job.config.reference_step_size)
-    j.max_steps = int(job.config.max_steps)
-    j.d_rgba8 = _ptr(job.out_rgba8)
-    j.d_rgba32f = _ptr(job.out_rgba32f)
-    j.d_counters = _ptr(job.counters)
+    fill_job(j, job.volume.handle.value, job.lut.handle.value, job.camera, job.light, job.config,
+             int(job.width), int(job.height), _ptr(job.out_rgba8), _ptr(job.out_rgba32f),
+             _ptr(job.counters))
     return j
 
 

@@ -16,8 +16,11 @@ clients at once:
   that arrive while others are on the GPU are admitted into the next batch,
   and up to ``slots`` batches overlap on the device (each on its own stream,
   its read-back overlapping the next batch's march);
-* each result is copied to pinned host memory and handed back as RGBA8 bytes
-  (bottom row first, as ``render()`` returns them).
+* transfer-function tables stay resident too, keyed by their content (an
+  orbit re-render reuses its session's table: no upload);
+* a batch writes its images into one device arena of its slot and comes back
+  in one copy to pinned host memory; each result is handed back as RGBA8
+  bytes (bottom row first, as ``render()`` returns them).
 
 ``SerialRenderer`` is the per-frame baseline: the same resident volumes, one
 request at a time, each rendered and read back before the next starts.
@@ -36,7 +39,7 @@ from typing import Dict, List, Optional
 import numpy as np
 
 from . import _native
-from .batch import BatchRenderer, DeviceLUT, DeviceVolume, RenderJob, Tuning, make_job_struct
+from .batch import BatchRenderer, DeviceLUT, DeviceVolume, Tuning, fill_job
 from .renderer import rgba_lut
 
 
@@ -136,6 +139,78 @@ class VolumeCache:
         return dv
 
 
+def tf_key(color_tf, opacity_tf) -> tuple:
+    """Content key of a transfer-function pair: equal keys give equal tables
+    (``rgba_lut`` depends on the control points and LUT sizes alone)."""
+    return (tuple((float(x), tuple(float(c) for c in rgb)) for x, rgb in color_tf.control_points),
+            tuple((float(x), float(a)) for x, a in opacity_tf.control_points),
+            int(color_tf.lut_size), int(opacity_tf.lut_size))
+
+
+class LutCache:
+    """Device LUTs keyed by transfer-function content (``tf_key``), LRU with a
+    fixed number of entries.  A LUT in use by a queued batch is pinned
+    (``acquire`` / ``release``) and never rewritten; an evicted LUT's memory
+    is reused for the next new table.  Used from one thread."""
+
+    def __init__(self, capacity: int = 1024):
+        self.capacity = capacity
+        self._luts: "collections.OrderedDict[tuple, DeviceLUT]" = collections.OrderedDict()
+        self._users: Dict[tuple, int] = collections.defaultdict(int)
+        self._free = _Pool(lambda n: DeviceLUT(rgba=np.zeros((n, 4), np.float32)))
+        self.hits = 0
+        self.misses = 0
+
+    def acquire(self, color_tf, opacity_tf):
+        key = tf_key(color_tf, opacity_tf)
+        lut = self._luts.get(key)
+        if lut is None:
+            table = rgba_lut(color_tf, opacity_tf)
+            self._evict()
+            lut = self._free.get(table.shape[0])
+            lut.update(table)
+            self._luts[key] = lut
+            self.misses += 1
+        else:
+            self._luts.move_to_end(key)
+            self.hits += 1
+        self._users[key] += 1
+        return key, lut
+
+    def release(self, key) -> None:
+        self._users[key] -= 1
+
+    def _evict(self) -> None:
+        while len(self._luts) >= self.capacity:
+            victim = next((k for k in self._luts if self._users.get(k, 0) == 0), None)
+            if victim is None:
+                return  # all in use: grow rather than stall
+            lut = self._luts.pop(victim)
+            self._users.pop(victim, None)
+            self._free.put(lut.size, lut)
+
+
+class _Arena:
+    """A slot's output images: one device buffer and one pinned host buffer,
+    grown (never shrunk) to the largest batch seen."""
+
+    def __init__(self, torch):
+        self.torch = torch
+        self.nbytes = 0
+        self.dev = None
+        self.host = None
+        self.view = None
+
+    def reserve(self, nbytes: int) -> None:
+        if nbytes <= self.nbytes:
+            return
+        n = 1 << max(20, (nbytes - 1).bit_length())
+        self.dev = self.torch.empty(n, dtype=self.torch.uint8, device="cuda")
+        self.host = self.torch.empty(n, dtype=self.torch.uint8).pin_memory()
+        self.view = self.host.numpy()
+        self.nbytes = n
+
+
 class _Pool:
     """Free lists of reusable objects keyed by a shape key."""
 
@@ -155,9 +230,14 @@ class RenderServer:
     """Continuous-batching render server (see module docstring)."""
 
     def __init__(self, budget_bytes: int = 40 << 30, max_batch: int = 64, slots: int = 3,
-                 tuning: Optional[Tuning] = None, brick_log2: int = 3):
+                 tuning: Optional[Tuning] = None, brick_log2: int = 3, loaders: int = 2,
+                 instrument: bool = False):
         import torch
         self.torch = torch
+        # instrument: CUDA events around every batch kernel and per-job sample
+        # counters (kernel_ms, samples, shaded) for roofline accounting
+        self.instrument = instrument
+        self.kernel_records: List[tuple] = []
         self.cache = VolumeCache(budget_bytes, brick_log2)
         self.max_batch = max_batch
         self.launcher = BatchRenderer(capacity=max_batch, slots=slots, tuning=tuning)
@@ -168,15 +248,16 @@ class RenderServer:
         self._loads: "queue.Queue[RenderRequest]" = queue.Queue()
         self._wake = threading.Event()
         self._stop = False
-        self._out_pool = _Pool(lambda wh: (torch.empty(wh[0] * wh[1] * 4, dtype=torch.uint8, device="cuda"),
-                                           torch.empty(wh[0] * wh[1] * 4, dtype=torch.uint8).pin_memory()))
-        self._lut_pool = _Pool(lambda n: DeviceLUT(rgba=np.zeros((n, 4), np.float32)))
+        self.luts = LutCache()
+        self._arenas = [_Arena(torch) for _ in range(slots)]
         self._structs = (_native.PvrJob * max_batch)()
         self._release_stream = torch.cuda.Stream()
         self.batches = 0
         self.batch_sizes: List[int] = []
-        self._threads = [threading.Thread(target=self._schedule, daemon=True, name="pvr-sched"),
-                         threading.Thread(target=self._load_loop, daemon=True, name="pvr-loader")]
+        self._counters = torch.zeros((slots, max_batch, 2), dtype=torch.int64, device="cuda")
+        self._threads = [threading.Thread(target=self._schedule, daemon=True, name="pvr-sched")]
+        self._threads += [threading.Thread(target=self._load_loop, daemon=True, name=f"pvr-loader{i}")
+                          for i in range(loaders)]
         for t in self._threads:
             t.start()
 
@@ -194,7 +275,8 @@ class RenderServer:
     def close(self) -> None:
         self._stop = True
         self._wake.set()
-        self._loads.put(None)
+        for _ in self._threads:
+            self._loads.put(None)
         for t in self._threads:
             t.join(timeout=30)
         self.torch.cuda.synchronize()
@@ -210,6 +292,7 @@ class RenderServer:
         dv.handle = None
 
     def _load_loop(self) -> None:
+        self.torch.cuda.set_device(self.torch.cuda.current_device())
         while True:
             req = self._loads.get()
             if req is None or self._stop:
@@ -233,16 +316,23 @@ class RenderServer:
                 return
 
     def _complete(self, slot: int) -> None:
-        ev, reqs, bufs, luts, vids = self._slot_busy[slot]
+        ev, reqs, offs, luts, vids = self._slot_busy[slot][:5]
         ev.synchronize()
         now = time.perf_counter()
-        for req, (wh, (dev, host)) in zip(reqs, bufs):
-            data = host.numpy().tobytes()
+        if self.instrument:
+            k0, k1 = self._slot_busy[slot][5]
+            per_job = self._counters[slot, :len(reqs)].tolist()
+            self.kernel_records.append((k0.elapsed_time(k1), sum(c[0] for c in per_job),
+                                        sum(c[1] for c in per_job),
+                                        [(r.width, r.height, r.value_scale, c[1])
+                                         for r, c in zip(reqs, per_job)]))
+        view = self._arenas[slot].view
+        for req, off in zip(reqs, offs):
+            data = view[off:off + req.width * req.height * 4].tobytes()
             req.done_at = now
             req.future.set_result(data)
-            self._out_pool.put(wh, (dev, host))
-        for lut in luts:
-            self._lut_pool.put(lut.size, lut)
+        for key in luts:
+            self.luts.release(key)
         for vid in vids:
             self.cache.release(vid)
         self._slot_busy[slot] = None
@@ -252,11 +342,9 @@ class RenderServer:
         self._slot_busy[slot] = None
         if busy is None:
             return
-        _, _, bufs, luts, vids = busy
-        for wh, pair in bufs:
-            self._out_pool.put(wh, pair)
-        for lut in luts:
-            self._lut_pool.put(lut.size, lut)
+        _, _, _, luts, vids = busy[:5]
+        for key in luts:
+            self.luts.release(key)
         for vid in vids:
             self.cache.release(vid)
 
@@ -278,27 +366,38 @@ class RenderServer:
             return
         reqs = [r for r, _ in ready]
         vids = [r.volume_id for r in reqs]
+        offs = []
         # resources belong to the slot from here on: released by _complete
         # or, on failure, by _abandon
-        self._slot_busy[slot] = (None, reqs, bufs, luts, vids)
+        self._slot_busy[slot] = (None, reqs, offs, luts, vids)
+        total = 0
+        for req in reqs:  # images packed at 256-byte aligned offsets
+            offs.append(total)
+            total += (req.width * req.height * 4 + 255) & ~255
+        arena = self._arenas[slot]
+        arena.reserve(total)
+        base = arena.dev.data_ptr()
+        cbase = self._counters[slot].data_ptr() if self.instrument else None
         for i, (req, dv) in enumerate(ready):
-            table = rgba_lut(req.color_tf, req.opacity_tf)
-            lut = self._lut_pool.get(table.shape[0])
-            lut.update(table)
-            luts.append(lut)
-            wh = (req.width, req.height)
-            dev, host = self._out_pool.get(wh)
-            bufs.append((wh, (dev, host)))
-            job = RenderJob(dv, lut, req.camera, req.light, req.config, req.width, req.height,
-                            out_rgba8=dev)
-            make_job_struct(job, self._structs[i])
+            key, lut = self.luts.acquire(req.color_tf, req.opacity_tf)
+            luts.append(key)
+            fill_job(self._structs[i], dv.handle.value, lut.handle.value, req.camera, req.light,
+                     req.config, int(req.width), int(req.height), base + offs[i], None,
+                     cbase + 16 * i if cbase is not None else None)
+        kev = None
+        if self.instrument:
+            kev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            with torch.cuda.stream(stream):
+                self._counters[slot].zero_()
+                kev[0].record(stream)
         self.launcher.render_structs(self._structs, len(reqs), stream=stream)
         ev = torch.cuda.Event()
         with torch.cuda.stream(stream):
-            for _, (dev, host) in bufs:
-                host.copy_(dev, non_blocking=True)
+            if kev:
+                kev[1].record(stream)
+            arena.host[:total].copy_(arena.dev[:total], non_blocking=True)
             ev.record(stream)
-        self._slot_busy[slot] = (ev, reqs, bufs, luts, vids)
+        self._slot_busy[slot] = (ev, reqs, offs, luts, vids, kev)
         self.batches += 1
         self.batch_sizes.append(len(reqs))
 
@@ -351,7 +450,7 @@ class SerialRenderer:
         self.launcher = BatchRenderer(capacity=1, slots=1, tuning=tuning)
         self.stream = torch.cuda.Stream()
         self._bufs = {}
-        self._lut = DeviceLUT(rgba=np.zeros((256, 4), np.float32))
+        self.luts = LutCache()
         self._struct = (_native.PvrJob * 1)()
 
     def _free_now(self, dv: DeviceVolume) -> None:
@@ -360,18 +459,20 @@ class SerialRenderer:
 
     def handle(self, req: RenderRequest) -> bytes:
         torch = self.torch
-        if req.kind == "load":
-            self.cache.insert(req.volume_id, req.volume, req.value_scale, self._free_now)
-        dv = self.cache.get(req.volume_id)
-        table = rgba_lut(req.color_tf, req.opacity_tf)
-        self._lut.update(table)
+        dv = None if req.kind == "load" else self.cache.get(req.volume_id)
+        if dv is None:  # a new volume, or one evicted earlier: load it first
+            if req.volume is None:
+                raise KeyError(f"volume {req.volume_id} is not resident")
+            dv = self.cache.insert(req.volume_id, req.volume, req.value_scale, self._free_now)
+        key, lut = self.luts.acquire(req.color_tf, req.opacity_tf)
+        self.luts.release(key)  # nothing is queued after this request returns
         wh = (req.width, req.height)
         if wh not in self._bufs:
             self._bufs[wh] = (torch.empty(wh[0] * wh[1] * 4, dtype=torch.uint8, device="cuda"),
                               torch.empty(wh[0] * wh[1] * 4, dtype=torch.uint8).pin_memory())
         dev, host = self._bufs[wh]
-        make_job_struct(RenderJob(dv, self._lut, req.camera, req.light, req.config, req.width,
-                                  req.height, out_rgba8=dev), self._struct[0])
+        fill_job(self._struct[0], dv.handle.value, lut.handle.value, req.camera, req.light,
+                 req.config, int(req.width), int(req.height), dev.data_ptr())
         self.launcher.render_structs(self._struct, 1, stream=self.stream)
         with torch.cuda.stream(self.stream):
             host.copy_(dev, non_blocking=True)
@@ -390,3 +491,91 @@ def latency_stats(reqs: List[RenderRequest]) -> dict:
     return {"n": int(lat.size), "p50_ms": float(np.percentile(lat, 50)),
             "p99_ms": float(np.percentile(lat, 99)), "max_ms": float(lat.max()),
             "mean_ms": float(lat.mean())}
+
+
+def _wait_until(t: float) -> None:
+    while True:
+        dt = t - time.perf_counter()
+        if dt <= 0:
+            return
+        time.sleep(dt - 0.0003 if dt > 0.0006 else 0.00005)
+
+
+def drive(impl, stream, timeout: float = 300.0):
+    """Replay a request stream [(arrival offset s, RenderRequest kwargs)] in
+    real time against a RenderServer or a SerialRenderer (open loop: a client
+    thread submits at the arrival times whatever the service does).  Returns
+    (requests, seconds from the first arrival to the last completion)."""
+    reqs = [RenderRequest(**kw) for _, kw in stream]
+    if not reqs:
+        return reqs, 0.0
+    if isinstance(impl, RenderServer):
+        t0 = time.perf_counter()
+        for (off, _), req in zip(stream, reqs):
+            _wait_until(t0 + off)
+            req.arrival = time.perf_counter()
+            impl.submit(req)
+        for req in reqs:
+            req.future.result(timeout=timeout)
+        return reqs, max(r.done_at for r in reqs) - t0
+    # serial: one worker thread serves a FIFO in order
+    q: "queue.Queue" = queue.Queue()
+
+    def worker():
+        while True:
+            req = q.get()
+            if req is None:
+                return
+            try:
+                req.future.set_result(impl.handle(req))
+            except Exception as e:
+                req.future.set_exception(e)
+            req.done_at = time.perf_counter()
+
+    th = threading.Thread(target=worker, daemon=True)
+    th.start()
+    t0 = time.perf_counter()
+    for (off, _), req in zip(stream, reqs):
+        _wait_until(t0 + off)
+        req.arrival = time.perf_counter()
+        q.put(req)
+    q.put(None)
+    for req in reqs:
+        req.future.result(timeout=timeout)
+    th.join()
+    return reqs, max(r.done_at for r in reqs) - t0
+
+
+def sustained_rate(impl, workload, rates, probe_s: float, seed: int, p99_ms: float = 20.0,
+                   refine: int = 0):
+    """Highest offered rate that `impl` serves with p99 latency <= p99_ms and
+    completions keeping up with arrivals: probes `rates` (ascending) up to the
+    first failure, then bisects `refine` times between the last passing and
+    the first failing rate.  Returns (rate or None, [probe results])."""
+    probes = []
+
+    def probe(rate, k):
+        stream = workload.requests(rate, probe_s, seed + k)
+        reqs, elapsed = drive(impl, stream)
+        st = latency_stats(reqs)
+        st.update(offered=rate, completed_per_s=len(reqs) / elapsed if elapsed else 0.0)
+        st["ok"] = bool(st.get("p99_ms", 1e9) <= p99_ms and st["completed_per_s"] >= 0.9 * rate)
+        probes.append(st)
+        return st["ok"]
+
+    best, fail = None, None
+    for rate in rates:
+        if not probe(rate, len(probes)):
+            fail = rate
+            break
+        best = rate
+    if best is not None and fail is not None:
+        lo, hi = best, fail
+        for _ in range(refine):
+            mid = 0.5 * (lo + hi)
+            if probe(mid, len(probes)):
+                lo = mid
+            else:
+                hi = mid
+        best = lo
+    return best, probes

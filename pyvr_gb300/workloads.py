@@ -131,11 +131,16 @@ def config_scale(dtype: str = "f32", n: int = 256, res: int = 1024, noise=None):
 
 
 def frame_inputs(volume: Volume, camera, light, config, lut: np.ndarray, width: int,
-                 height: int, value_scale: float = 1.0) -> dict:
+                 height: int, value_scale: float = 1.0, batch_camera: bool = False) -> dict:
     """Everything one frame depends on, as the uniforms/textures the reference
-    renderer would set (renderer.py:107-172, 303-316), in a plain dict."""
-    from .renderer import camera_uniforms
-    view, proj, pos = camera_uniforms(camera, width, height)
+    renderer would set (renderer.py:107-172, 303-316), in a plain dict.
+    batch_camera: camera matrices as the batch path computes them (native
+    double-precision setup) instead of the ``Camera`` methods'."""
+    if batch_camera:
+        from .batch import job_camera_uniforms as uniforms
+    else:
+        from .renderer import camera_uniforms as uniforms
+    view, proj, pos = uniforms(camera, width, height)
     return dict(width=width, height=height, view=view, proj=proj, cam_pos=pos,
                 volume=volume.data, normals=volume.normals, value_scale=value_scale,
                 bmin=volume.min_bounds, bmax=volume.max_bounds, lut=lut,

@@ -95,7 +95,7 @@ def _run_batch(scenes, tuning=None, brick_log2=3, repeat=1):
 def _oracle(s):
     lut = rgba_lut(s["ctf"], s["otf"])
     return oracle.render(W.frame_inputs(s["vol"], s["cam"], s["light"], s["cfg"], lut, s["w"], s["h"],
-                                        s["vs"]))
+                                        s["vs"], batch_camera=True))
 
 
 def test_batch_of_mixed_jobs_matches_oracle():

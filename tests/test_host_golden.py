@@ -32,6 +32,36 @@ def test_camera_matches_reference(i):
     np.testing.assert_array_equal(cam.get_projection_matrix(float(p[8])), G["camera_proj"][i])
 
 
+@pytest.mark.parametrize("i", range(len(G["camera_params"])))
+def test_batch_camera_setup_matches_reference(i, native_lib):
+    # the batch path's native double-precision camera setup: the reference's
+    # float32 matrices to float32 rounding
+    from pyvr_gb300.batch import job_camera_uniforms
+    p = G["camera_params"][i]
+    view, proj, pos = job_camera_uniforms(_camera(p), float(p[8]), 1.0)
+    np.testing.assert_allclose(pos, G["camera_pos"][i], rtol=0, atol=2e-6)
+    np.testing.assert_allclose(view, G["camera_view"][i], rtol=0, atol=2e-6)
+    np.testing.assert_allclose(proj, G["camera_proj"][i], rtol=2e-7, atol=0)
+
+
+def test_batch_camera_setup_rejects_bad_cameras(native_lib):
+    import ctypes
+    f3 = ctypes.c_float * 3
+    f16 = ctypes.c_float * 16
+    args = lambda **kw: [f3(0, 0, 0), 0.0, 0.0, 0.0, kw.get("dist", 3.0), f3(*kw.get("pos", (1, 0, 0))),
+                         f3(0, 0, 1), kw.get("fov", 0.785), 0.1, kw.get("far", 100.0), 1.0,
+                         f16(), f16(), f3()]
+    assert native_lib.pvr_camera_spherical(*args()) == 0
+    for bad in (dict(dist=0.0), dict(dist=-1.0), dict(pos=(0, 0, 0)), dict(fov=0.0), dict(fov=3.2),
+                dict(far=0.05)):
+        assert native_lib.pvr_camera_spherical(*args(**bad)) == 1, bad  # PVR_ERR_VALUE
+    # up parallel to the view direction: no basis to give
+    bad = args(pos=(0, 0, 2))
+    bad[6] = f3(0, 0, 1)
+    assert native_lib.pvr_camera_spherical(*bad) == 1
+    assert b"parallel" in native_lib.pvr_last_error()
+
+
 def test_camera_default_position():
     # reference tests/test_camera/test_control.py:22-32: default init -> [0,0,3]-like pins
     cam = Camera.from_spherical(np.zeros(3, np.float32), np.pi / 4, np.pi / 6, 0.0, 3.0)

@@ -33,10 +33,7 @@ def _run(budget, n_req=160):
     got = [f.result(timeout=120) for f in futs]
     want = []
     for _, kw in stream:
-        req = RenderRequest(**kw)
-        if req.kind == "render" and serial.cache.get(req.volume_id) is None:
-            req.kind = "load"  # the serial cache may have evicted / never seen it
-        want.append(serial.handle(req))
+        want.append(serial.handle(RenderRequest(**kw)))
     stats = dict(batches=server.batches, sizes=list(server.batch_sizes),
                  evictions=server.cache.evictions, loads=server.cache.loads, lat=latency_stats(reqs))
     server.close()
@@ -60,7 +57,8 @@ def test_server_results_equal_results_alone():
                    max_bounds=vol.max_bounds)
         lut = rgba_lut(kw["color_tf"], kw["opacity_tf"])
         o8, _, _ = oracle.render(W.frame_inputs(v, kw["camera"], kw["light"], kw["config"], lut,
-                                                kw["width"], kw["height"], vs), want_float=False)
+                                                kw["width"], kw["height"], vs, batch_camera=True),
+                                 want_float=False)
         assert g == o8.tobytes()
 
 
