@@ -211,6 +211,21 @@ int pvr_batch_render(pvr_batch *b, const pvr_job *jobs, int n, void *stream);
 /* Wait for every batch queued on this launcher. */
 int pvr_batch_synchronize(pvr_batch *b);
 
+/* Batch render that allocates nothing (no counterpart in the reference,
+ * which renders one frame per call): the persistent batch march of
+ * pvr_batch_render without a pvr_batch launcher, for callers that may not
+ * allocate or free device memory (a process whose device memory all belongs
+ * to its own pool, a frame loop with a fixed budget, a host that must not add
+ * the device-wide synchronisation of cudaFree).  Its scratch -- one tile
+ * counter per launch of up to 96 jobs, cleared to 0 by the call on `stream`
+ * -- is a static 256-byte device array, so a call takes at most 6144 jobs
+ * (PVR_ERR_VALUE beyond, nothing queued).  Calls whose work may overlap on a
+ * device race on that array: keep them on one stream or order them.  The
+ * first call on a device looks the array up (cudaGetSymbolAddress): make it
+ * outside stream capture.  tuning: NULL for the default; stream: NULL for
+ * the default stream. */
+int pvr_batch_render_static(const pvr_job *jobs, int n, const pvr_tuning *tuning, void *stream);
+
 /* Orbit camera setup on the host in double precision: Camera.from_spherical
  * + get_camera_vectors / get_view_matrix / get_projection_matrix(aspect)
  * (pyvr/camera/control.py:238-351, pyvr/camera/camera.py:292-369), giving the

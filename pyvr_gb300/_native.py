@@ -126,6 +126,7 @@ SIGNATURES = {
     "pvr_batch_get_tuning": (_I, [_VP, _VP]),
     "pvr_batch_render": (_I, [_VP, _VP, _I, _VP]),
     "pvr_batch_synchronize": (_I, [_VP]),
+    "pvr_batch_render_static": (_I, [_VP, _I, _VP, _VP]),
     "pvr_camera_spherical": (_I, [_FP, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                   _FP, _FP, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                   ctypes.c_double, _FP, _FP, _FP]),

@@ -278,3 +278,14 @@ class BatchRenderer:
             self.close()
         except Exception:
             pass
+
+
+def render_static(structs, n: int, tuning: Optional["Tuning"] = None, stream=None) -> None:
+    """Queue n prepared PvrJob structs through ``pvr_batch_render_static``:
+    the batch march with no launcher and no memory allocation (scratch in a
+    static device array; at most 6144 jobs per call; calls that may overlap on
+    the GPU must be ordered, e.g. on one stream)."""
+    t = tuning.c() if tuning is not None else None
+    s = getattr(stream, "cuda_stream", stream)
+    check(_lib().pvr_batch_render_static(ctypes.cast(structs, ctypes.c_void_p), int(n),
+                                         ctypes.addressof(t) if t is not None else None, s))

@@ -1,0 +1,143 @@
+// pvr_batch_render_static: the persistent batch march without any memory
+// allocation in the call or in a handle it needs.
+//
+// pvr_batch_render takes a pvr_batch launcher, whose creation allocates a
+// device tile counter per slot (cudaMalloc) and whose destruction frees them
+// (cudaFree synchronises the whole device).  Some callers cannot do either:
+// an application that hands the entire device memory to its own pool, a frame
+// loop with a fixed memory budget that must not fail on an allocation half
+// way through, or a host that must not add device-wide synchronisation.  This
+// entry point needs only the pvr_volume / pvr_lut handles and the output
+// buffers the caller already owns; the one piece of scratch memory the kernel
+// needs -- a tile counter per launch, which must read 0 when the launch
+// starts -- lives in a fixed static device array, cleared by the call itself
+// (cudaMemsetAsync on the caller's stream) before the launches that use it.
+//
+// Limits and rules:
+//  * at most kStaticCounters launches of kMaxLaunchJobs jobs per call
+//    (64 x 96 = 6144 jobs); larger calls fail with PVR_ERR_VALUE before
+//    anything is queued;
+//  * the counters are shared by every call on a device: two calls whose work
+//    may overlap on the GPU (different streams, or different host threads
+//    without ordering) race on them and can skip or repeat tiles.  Issue the
+//    calls on one stream, or order them with events;
+//  * the address of the static array is looked up once per device
+//    (cudaGetSymbolAddress, which also loads this module on that device);
+//    make the first call on each device outside stream capture.
+#include <algorithm>
+#include <atomic>
+#include <cstring>
+#include <string>
+
+#include "pvr_internal.h"
+
+namespace {
+
+constexpr int kStaticCounters = 64;  // 256 bytes of scratch per device
+constexpr int kMaxDevices = 64;
+
+__device__ __align__(256) static int g_tile_counters[kStaticCounters];
+
+std::atomic<int *> g_counter_addr[kMaxDevices];
+
+int counters_for_device(int device, int **out) {
+    if (device < 0 || device >= kMaxDevices) return pvr::fail(PVR_ERR_VALUE, "device ordinal %d out of range", device);
+    int *p = g_counter_addr[device].load(std::memory_order_acquire);
+    if (!p) {
+        void *addr = nullptr;
+        PVR_CUDA(cudaGetSymbolAddress(&addr, g_tile_counters));
+        p = static_cast<int *>(addr);
+        g_counter_addr[device].store(p, std::memory_order_release);
+    }
+    *out = p;
+    return PVR_OK;
+}
+
+bool tuning_ok(const pvr::Tuning &t) {
+    return t.tile_w > 0 && t.tile_h > 0 && t.tile_w % 8 == 0 && t.tile_h % 4 == 0 &&
+           t.tile_w * t.tile_h == pvr::kBatchThreads && (t.steps_per_iter == 1 || t.steps_per_iter == 4) &&
+           t.blocks_per_sm >= 0 && t.blocks_per_sm <= 16;
+}
+
+}  // namespace
+
+using pvr::fail;
+
+extern "C" int pvr_batch_render_static(const pvr_job *jobs, int n, const pvr_tuning *tuning, void *stream) {
+    constexpr int kMaxJobs = kStaticCounters * pvr::kMaxLaunchJobs;
+    if (n < 0 || n > kMaxJobs)
+        return fail(PVR_ERR_VALUE,
+                    "pvr_batch_render_static: %d jobs; at most %d per call (%d launches of %d jobs, "
+                    "one static tile counter each)",
+                    n, kMaxJobs, kStaticCounters, pvr::kMaxLaunchJobs);
+    if (n > 0 && !jobs) return fail(PVR_ERR_VALUE, "jobs is NULL");
+    if (n == 0) return PVR_OK;
+    pvr::Tuning t;
+    if (tuning) {
+        t.tile_w = tuning->tile_w;
+        t.tile_h = tuning->tile_h;
+        t.steps_per_iter = tuning->steps_per_iter;
+        t.blocks_per_sm = tuning->blocks_per_sm;
+        if (!tuning_ok(t))
+            return fail(PVR_ERR_VALUE, "tuning: tile_w%%8==0, tile_h%%4==0, tile_w*tile_h==256, "
+                                       "steps_per_iter in {1,4}, blocks_per_sm in 0..16");
+    }
+    if (!jobs[0].volume) return fail(PVR_ERR_VALUE, "job 0 without volume or LUT");
+    const int log2b = jobs[0].volume->log2b;
+    for (int i = 0; i < n; ++i) {
+        if (!jobs[i].volume || !jobs[i].lut) return fail(PVR_ERR_VALUE, "job %d without volume or LUT", i);
+        if (jobs[i].volume->log2b != log2b)
+            return fail(PVR_ERR_VALUE, "all volumes of a batch must share one brick size");
+    }
+    int device = 0, sms = 0;
+    PVR_CUDA(cudaGetDevice(&device));
+    PVR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    int *counters = nullptr;
+    if (int rc = counters_for_device(device, &counters)) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    const void *fn = pvr::batch_kernel(log2b, t);
+    // job tables are built on the host stack: the launch copies its parameters
+    pvr::BatchParams p;
+    const int launches = (n + pvr::kMaxLaunchJobs - 1) / pvr::kMaxLaunchJobs;
+    // validate every job before anything is queued
+    for (int c = 0; c < launches; ++c) {
+        const int i0 = c * pvr::kMaxLaunchJobs, m = std::min(pvr::kMaxLaunchJobs, n - i0);
+        long long total = 0;
+        for (int i = 0; i < m; ++i) {
+            if (int rc = pvr::fill_job(jobs[i0 + i], t.tile_w, t.tile_h, p.jobs[i])) {
+                const std::string why = pvr_last_error();
+                return fail(rc, "job %d: %s", i0 + i, why.c_str());
+            }
+            total += (long long)p.jobs[i].tiles_x * p.jobs[i].tiles_y;
+        }
+        if (total > (1LL << 30)) return fail(PVR_ERR_VALUE, "launch %d has too many tiles", c);
+    }
+    PVR_CUDA(cudaMemsetAsync(counters, 0, (size_t)launches * sizeof(int), st));
+    for (int c = 0; c < launches; ++c) {
+        const int i0 = c * pvr::kMaxLaunchJobs, m = std::min(pvr::kMaxLaunchJobs, n - i0);
+        long long total = 0;
+        int max_lut = 1;
+        for (int i = 0; i < m; ++i) {
+            pvr::fill_job(jobs[i0 + i], t.tile_w, t.tile_h, p.jobs[i]);
+            p.jobs[i].tile_base = (int)total;
+            p.tile_base[i] = (int)total;
+            total += (long long)p.jobs[i].tiles_x * p.jobs[i].tiles_y;
+            max_lut = std::max(max_lut, jobs[i0 + i].lut->size);
+        }
+        p.njobs = m;
+        p.total_tiles = (int)total;
+        p.tile_w = t.tile_w;
+        p.tile_h = t.tile_h;
+        int lut_smem = 256;
+        while (lut_smem < max_lut && lut_smem < 2048) lut_smem *= 2;
+        p.lut_smem_entries = lut_smem;
+        p.work = counters + c;
+        int per_sm = t.blocks_per_sm;
+        const int fit = pvr::max_batch_blocks_per_sm(log2b, t, lut_smem);
+        if (per_sm <= 0 || per_sm > fit) per_sm = std::max(1, fit);
+        void *args[] = {&p};
+        PVR_CUDA(cudaLaunchKernel(fn, dim3(sms * per_sm), dim3(pvr::kBatchThreads), args,
+                                  pvr::batch_smem_bytes(lut_smem), st));
+    }
+    return PVR_OK;
+}
