@@ -238,11 +238,6 @@ int pvr_camera_spherical(const float target[3], double azimuth, double elevation
                          double near_plane, double far_plane, double aspect, float view_out[16],
                          float proj_out[16], float pos_out[3]);
 
-/* Page-locked host memory mapped for the device (a job's d_rgba8 may point
- * at device_ptr: the kernel then writes the image straight to host memory). */
-int pvr_host_buffer_create(long long bytes, void **host_ptr, void **device_ptr);
-int pvr_host_buffer_free(void *host_ptr);
-
 #ifdef __cplusplus
 }
 #endif

@@ -130,8 +130,6 @@ SIGNATURES = {
     "pvr_camera_spherical": (_I, [_FP, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                   _FP, _FP, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                   ctypes.c_double, _FP, _FP, _FP]),
-    "pvr_host_buffer_create": (_I, [_LL, ctypes.POINTER(_VP), ctypes.POINTER(_VP)]),
-    "pvr_host_buffer_free": (_I, [_VP]),
 }
 
 PVR_NORMALS_NONE, PVR_NORMALS_GIVEN, PVR_NORMALS_DEVICE = 0, 1, 2

@@ -92,26 +92,3 @@ extern "C" int pvr_camera_spherical(const float target[3], double azimuth, doubl
     pos_out[2] = (float)pos.z;
     return PVR_OK;
 }
-
-// Page-locked host memory mapped into the device address space: the batch
-// kernel writes RGBA8 results straight into it (no separate read-back copy).
-extern "C" int pvr_host_buffer_create(long long bytes, void **host_ptr, void **device_ptr) {
-    if (!host_ptr || !device_ptr || bytes <= 0) return pvr::fail(PVR_ERR_VALUE, "invalid host buffer request");
-    *host_ptr = *device_ptr = nullptr;
-    void *h = nullptr;
-    PVR_CUDA(cudaHostAlloc(&h, (size_t)bytes, cudaHostAllocMapped | cudaHostAllocPortable));
-    void *d = nullptr;
-    cudaError_t e = cudaHostGetDevicePointer(&d, h, 0);
-    if (e != cudaSuccess) {
-        cudaFreeHost(h);
-        return pvr::cuda_fail(e, "cudaHostGetDevicePointer");
-    }
-    *host_ptr = h;
-    *device_ptr = d;
-    return PVR_OK;
-}
-
-extern "C" int pvr_host_buffer_free(void *host_ptr) {
-    if (host_ptr) cudaFreeHost(host_ptr);
-    return PVR_OK;
-}
