@@ -60,7 +60,8 @@ def parse_args():
     ap.add_argument("--serving-volumes", type=int, default=32)
     ap.add_argument("--serving-max-dim", type=int, default=512)
     # smaller cases for profiling captures
-    ap.add_argument("--only", choices=["all", "plain", "serving"], default="all")
+    ap.add_argument("--only", choices=["all", "plain", "serving", "diff"], default="all")
+    ap.add_argument("--diff-steps", type=int, default=200, help="Adam steps of the differentiation section")
     ap.add_argument("--storages", default=",".join(DTYPES))
     ap.add_argument("--cameras", type=int, default=16)
     ap.add_argument("--skip-cpu", action="store_true")
@@ -265,6 +266,75 @@ def serving_section(args, torch):
 
 
 # ---------------------------------------------------------------------------
+# Differentiation (nested section)
+# ---------------------------------------------------------------------------
+
+def diff_section(args, torch):
+    """Transfer-function recovery: 128^3 FP32 value noise (seed 3), 8 views at
+    512^2 rendered as float RGBA, MSE against targets rendered from another
+    seeded TF, Adam on the 256-entry LUT; each step = forward + loss +
+    hand-written backward + Adam update, timed with CUDA events."""
+    import numpy as np
+    from pyvr_gb300 import Camera, Light, RenderConfig, compute_normal_volume
+    from pyvr_gb300 import workloads as W
+    from pyvr_gb300.diff import DiffScene, render_views
+    from pyvr_gb300.renderer import rgba_lut
+    n, res, views = 128, 512, 8
+    data = W.value_noise((n, n, n), seed=3).astype(np.float32)
+    nrm = torch.tensor(compute_normal_volume(data), device="cuda")
+    vol = torch.tensor(data, device="cuda")
+    rng = np.random.default_rng(3)
+    ctf = W.standin_colormap(3)
+    lut0 = torch.tensor(rgba_lut(ctf, W.random_opacity(rng, 8, 0.3)), device="cuda")
+    lut_t = torch.tensor(rgba_lut(ctf, W.random_opacity(rng, 8, 0.3)), device="cuda")
+    cams = [Camera.from_spherical(np.zeros(3, np.float32), 2 * np.pi * k / views, np.pi / 6, 0.0, 3.0)
+            for k in range(views)]
+    scene = DiffScene(cams, Light.directional([1, -1, 0], 0.2, 0.8), RenderConfig.balanced(), res, res)
+    with torch.no_grad():
+        target, steps_t = render_views(vol, lut_t, scene, nrm, return_steps=True)
+
+    def run(n_steps, with_volume):
+        lut = lut0.clone().requires_grad_(True)
+        v = vol.clone().requires_grad_(with_volume)
+        opt = torch.optim.Adam([lut], lr=0.01)
+        ev = []
+        losses = []
+        for _ in range(n_steps):
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+            e[0].record()
+            opt.zero_grad(set_to_none=True)
+            img = render_views(v, lut, scene, nrm)
+            e[1].record()
+            loss = ((img - target) ** 2).mean()
+            loss.backward()
+            e[2].record()
+            opt.step()
+            with torch.no_grad():
+                lut.clamp_(0.0, 1.0)
+            e[3].record()
+            ev.append(e)
+            losses.append(loss.detach())
+        torch.cuda.synchronize()
+        step = [a.elapsed_time(d) for a, _, _, d in ev]
+        fwd = [a.elapsed_time(b) for a, b, _, _ in ev]
+        bwd = [b.elapsed_time(c) for _, b, c, _ in ev]
+        return step, fwd, bwd, [float(x) for x in losses]
+
+    run(args.warmup, False)
+    step, fwd, bwd, losses = run(args.diff_steps, False)
+    vstep, vfwd, vbwd, _ = run(max(args.warmup, 10), True)
+    return {"ms_per_step": statistics.mean(step), "ms_per_step_median": statistics.median(step),
+            "forward_ms": statistics.mean(fwd), "backward_ms": statistics.mean(bwd), "steps": args.diff_steps,
+            "loss_first": losses[0], "loss_last": losses[-1],
+            "with_volume_gradient": {"ms_per_step": statistics.mean(vstep), "forward_ms": statistics.mean(vfwd),
+                                     "backward_ms": statistics.mean(vbwd)},
+            "mean_loop_iterations_per_ray": float(steps_t.float().mean()),
+            "config": {"volume": "128^3 FP32 value noise seed 3 (normals constant)", "views": views,
+                       "resolution": f"{res}x{res}", "lut": 256, "render_config": "balanced",
+                       "loss": "MSE over float RGBA", "optimizer": "Adam lr 0.01 on the LUT, clamped to [0,1]"}}
+
+
+# ---------------------------------------------------------------------------
 # Plain per-frame renderer (nested section)
 # ---------------------------------------------------------------------------
 
@@ -384,9 +454,10 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
     plain = plain_section(args, torch) if args.only in ("all", "plain") else None
-    if args.only == "plain":
+    diff = diff_section(args, torch) if args.only in ("all", "diff") else None
+    if args.only in ("plain", "diff"):
         if rank == 0:
-            print(json.dumps({"plain": plain}))
+            print(json.dumps({"plain": plain, "differentiation": diff}))
         return
     s = serving_section(args, torch)
     value, serial_value = s["value"], s["serial_value"]
@@ -424,7 +495,7 @@ def run_ours(args):
                 "e2e": {"value": value, "unit": "renders/s", "h2d_bytes_per_step": s["h2d"],
                         "d2h_bytes_per_step": s["d2h"]},
                 "gpu_launches": s["batches"],
-                "plain": plain}
+                "plain": plain, "differentiation": diff}
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -226,6 +226,46 @@ int pvr_batch_synchronize(pvr_batch *b);
  * the default stream. */
 int pvr_batch_render_static(const pvr_job *jobs, int n, const pvr_tuning *tuning, void *stream);
 
+/* ---- Differentiable march (no counterpart in the reference) ----------
+ * Gradients of an image loss with respect to the RGBA LUT and the voxel
+ * values of an FP32 volume, for several views of one scene.  Device
+ * pointers throughout; the scene's `views` array is on the host. */
+typedef struct {
+    float view[16];        /* Camera.get_view_matrix() as float32, row-major bytes */
+    float proj[16];        /* Camera.get_projection_matrix(width / height) */
+    float camera_pos[3];
+} pvr_diff_view;
+
+typedef struct {
+    const float *volume;   /* device (D,H,W) float32, C order */
+    const float *normals;  /* device (D,H,W,3) float32, or NULL: normal = (density, 0, 0) */
+    int d, h, w;
+    float value_scale;
+    const float *lut;      /* device (lut_size, 4) float32 RGBA, lut_size <= 2048 */
+    int lut_size;
+    float min_bounds[3], max_bounds[3];
+    float light_pos[3], light_target[3];
+    float ambient, diffuse;
+    float step_size, reference_step_size;
+    int max_steps;
+    int width, height;
+    int n_views;
+    const pvr_diff_view *views;
+} pvr_diff_scene;
+
+/* Forward: d_image = n_views x H x W float RGBA (the renderer's float image,
+ * bit for bit), d_steps = n_views x H x W loop iterations executed (kept for
+ * the backward; no per-sample state is stored). */
+int pvr_diff_forward(const pvr_diff_scene *scene, float *d_image, int *d_steps, void *stream);
+
+/* Backward of pvr_diff_forward: given dL/dimage, ADDS dL/dLUT (lut_size x 4)
+ * into d_grad_lut and dL/dvoxel (D x H x W) into d_grad_volume (either may
+ * be NULL: not computed).  Transmittance is rebuilt by a reverse march over
+ * each ray; normals are held constant. */
+int pvr_diff_backward(const pvr_diff_scene *scene, const float *d_image, const int *d_steps,
+                      const float *d_grad_image, float *d_grad_lut, float *d_grad_volume,
+                      void *stream);
+
 /* Orbit camera setup on the host in double precision: Camera.from_spherical
  * + get_camera_vectors / get_view_matrix / get_projection_matrix(aspect)
  * (pyvr/camera/control.py:238-351, pyvr/camera/camera.py:292-369), giving the

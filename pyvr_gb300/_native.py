@@ -127,6 +127,8 @@ SIGNATURES = {
     "pvr_batch_render": (_I, [_VP, _VP, _I, _VP]),
     "pvr_batch_synchronize": (_I, [_VP]),
     "pvr_batch_render_static": (_I, [_VP, _I, _VP, _VP]),
+    "pvr_diff_forward": (_I, [_VP, _VP, _VP, _VP]),
+    "pvr_diff_backward": (_I, [_VP, _VP, _VP, _VP, _VP, _VP, _VP]),
     "pvr_camera_spherical": (_I, [_FP, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                   _FP, _FP, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                   ctypes.c_double, _FP, _FP, _FP]),
@@ -138,6 +140,21 @@ PVR_NORMALS_NONE, PVR_NORMALS_GIVEN, PVR_NORMALS_DEVICE = 0, 1, 2
 class PvrTuning(ctypes.Structure):
     """pvr_tuning of include/pyvr_gb300.h."""
     _fields_ = [("tile_w", _I), ("tile_h", _I), ("steps_per_iter", _I), ("blocks_per_sm", _I)]
+
+
+class PvrDiffView(ctypes.Structure):
+    """pvr_diff_view of include/pyvr_gb300.h."""
+    _fields_ = [("view", _F * 16), ("proj", _F * 16), ("camera_pos", _F * 3)]
+
+
+class PvrDiffScene(ctypes.Structure):
+    """pvr_diff_scene of include/pyvr_gb300.h."""
+    _fields_ = [("volume", _VP), ("normals", _VP), ("d", _I), ("h", _I), ("w", _I),
+                ("value_scale", _F), ("lut", _VP), ("lut_size", _I),
+                ("min_bounds", _F * 3), ("max_bounds", _F * 3),
+                ("light_pos", _F * 3), ("light_target", _F * 3), ("ambient", _F), ("diffuse", _F),
+                ("step_size", _F), ("reference_step_size", _F), ("max_steps", _I),
+                ("width", _I), ("height", _I), ("n_views", _I), ("views", _VP)]
 
 
 class PvrJob(ctypes.Structure):
