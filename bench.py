@@ -29,6 +29,7 @@ all host cores) serving the same request mix, on bounded row bands.
 
 import argparse
 import ctypes
+import dataclasses
 import json
 import os
 import statistics
@@ -60,7 +61,7 @@ def parse_args():
     ap.add_argument("--serving-volumes", type=int, default=32)
     ap.add_argument("--serving-max-dim", type=int, default=512)
     # smaller cases for profiling captures
-    ap.add_argument("--only", choices=["all", "plain", "serving", "diff"], default="all")
+    ap.add_argument("--only", choices=["all", "plain", "serving", "diff", "batching"], default="all")
     ap.add_argument("--diff-steps", type=int, default=200, help="Adam steps of the differentiation section")
     ap.add_argument("--storages", default=",".join(DTYPES))
     ap.add_argument("--cameras", type=int, default=16)
@@ -266,6 +267,81 @@ def serving_section(args, torch):
 
 
 # ---------------------------------------------------------------------------
+# Batching (nested section)
+# ---------------------------------------------------------------------------
+
+def batching_section(args, torch):
+    """64 uneven renders (volumes 32..384 per axis, u8/f16/f32, 128^2..1024^2,
+    random cameras and TFs) in one persistent launch replayed as a CUDA graph,
+    with the autotuner's tile shape / brick size / steps per iteration /
+    blocks per SM; beside it the default tuning and the same 64 renders as 64
+    single-render launches."""
+    from pyvr_gb300 import workloads as W
+    from pyvr_gb300.autotune import _Bench, autotune
+    from pyvr_gb300.batch import BatchRenderer, Tuning
+    scenes = W.config_batching(64, noise=W.value_noise_device)
+    t_tune = time.perf_counter()
+    best, results = autotune(scenes, repeats=3, use_cache=False)
+    tune_s = time.perf_counter() - t_tune
+    bench = _Bench(scenes)
+    counters = torch.zeros((len(scenes), 2), dtype=torch.int64, device="cuda")
+
+    def timed(tuning, per_frame=False, count=False):
+        jobs = bench.jobs(tuning.brick_log2)
+        if count:
+            for i, j in enumerate(jobs):
+                j.counters = counters[i]
+        br = BatchRenderer(capacity=len(jobs), slots=2, tuning=tuning)
+        st = bench.stream
+
+        def launch():
+            if per_frame:
+                for j in jobs:
+                    br.render([j], stream=st)
+            else:
+                br.render(jobs, stream=st)
+
+        for _ in range(args.warmup):
+            launch()
+        if count:
+            counters.zero_()
+            launch()
+            st.synchronize()
+            for j in jobs:  # count one batch only
+                j.counters = None
+        st.synchronize()
+        ev = []
+        for _ in range(args.steps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(st)
+            launch()
+            b.record(st)
+            ev.append((a, b))
+        st.synchronize()
+        br.close()
+        return statistics.mean(a.elapsed_time(b) for a, b in ev)
+
+    ms_best = timed(best, count=True)
+    per = counters.cpu().numpy()
+    default = Tuning()
+    ms_default = timed(default)
+    ms_frames = timed(best, per_frame=True)
+    dtypes = [s["dtype"] for s in scenes]
+    shaded_bytes = sum(int(c[1]) * BYTES_PER_SAMPLE[dt] for c, dt in zip(per, dtypes))
+    peak, peak_kind = measured_peaks()
+    achieved = shaded_bytes / (ms_best / 1000.0) / 1e9
+    return {"renders_per_s": len(scenes) / (ms_best / 1000.0), "ms_per_batch": ms_best,
+            "default_tuning_ms_per_batch": ms_default, "per_frame_launches_ms": ms_frames,
+            "tuning": dataclasses.asdict(best), "tuning_search_s": tune_s, "candidates": len(results),
+            "candidate_ms": sorted(round(ms, 3) for _, ms in results)[:5],
+            "samples_inbox": int(per[:, 0].sum()), "samples_shaded": int(per[:, 1].sum()),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind, "kernel": "march_batch_kernel"},
+            "config": {"renders": len(scenes), "volumes": "32..384 per axis log-uniform, u8/f16/f32 value noise",
+                       "resolutions": "128^2..1024^2", "render_config": "balanced", "steps": args.steps}}
+
+
+# ---------------------------------------------------------------------------
 # Differentiation (nested section)
 # ---------------------------------------------------------------------------
 
@@ -455,9 +531,10 @@ def run_ours(args):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
     plain = plain_section(args, torch) if args.only in ("all", "plain") else None
     diff = diff_section(args, torch) if args.only in ("all", "diff") else None
-    if args.only in ("plain", "diff"):
+    batching = batching_section(args, torch) if args.only in ("all", "batching") else None
+    if args.only in ("plain", "diff", "batching"):
         if rank == 0:
-            print(json.dumps({"plain": plain, "differentiation": diff}))
+            print(json.dumps({"plain": plain, "differentiation": diff, "batching_c3": batching}))
         return
     s = serving_section(args, torch)
     value, serial_value = s["value"], s["serial_value"]
@@ -495,7 +572,7 @@ def run_ours(args):
                 "e2e": {"value": value, "unit": "renders/s", "h2d_bytes_per_step": s["h2d"],
                         "d2h_bytes_per_step": s["d2h"]},
                 "gpu_launches": s["batches"],
-                "plain": plain, "differentiation": diff}
+                "plain": plain, "batching_c3": batching, "differentiation": diff}
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -149,13 +149,15 @@ def frame_inputs(volume: Volume, camera, light, config, lut: np.ndarray, width: 
                 ambient=light.ambient_intensity, diffuse=light.diffuse_intensity)
 
 
-def config_batching(n: int = 64, max_dim: int = 384, resolutions=(128, 256, 512, 1024)):
+def config_batching(n: int = 64, max_dim: int = 384, resolutions=(128, 256, 512, 1024), noise=None):
     """n uneven renders: per instance i (seed i) volume extents drawn
     log-uniformly from 32..max_dim per axis (non-cubic), storage uniform over
     uint8/float16/float32, value noise, resolution uniform over the given
     squares, a random camera on a sphere of radius 2.5-4 around the box, and
     a random TF (4-12 opacity points, one of the 12 stand-in colour maps).
-    Normals are left to the device (numpy.gradient semantics)."""
+    Normals are left to the device (numpy.gradient semantics).  noise:
+    the value-noise generator (shape, seed) -> array (default value_noise)."""
+    noise = noise or value_noise
     scenes = []
     for i in range(n):
         rng = np.random.default_rng(i)
@@ -169,7 +171,7 @@ def config_batching(n: int = 64, max_dim: int = 384, resolutions=(128, 256, 512,
         el = float(np.arcsin(np.clip(v[2], -1, 1)))
         otf = random_opacity(rng, int(rng.integers(4, 13)), 0.3)
         ctf = standin_colormap(int(rng.integers(0, N_STANDIN_COLORMAPS)))
-        data = to_storage(value_noise(dims, seed=i), dtype)
+        data = to_storage(noise(dims, i), dtype)
         vol = Volume(data=data, min_bounds=np.array([-1.0, -1.0, -1.0], np.float32),
                      max_bounds=np.array([1.0, 1.0, 1.0], np.float32))
         cam = Camera.from_spherical(target=np.zeros(3, np.float32), azimuth=az, elevation=el, roll=0.0,
@@ -184,18 +186,19 @@ def config_batching(n: int = 64, max_dim: int = 384, resolutions=(128, 256, 512,
 # Serving workload
 # ---------------------------------------------------------------------------
 
-def value_noise_device(n: int, seed: int) -> np.ndarray:
-    """value_noise((n, n, n), seed) by the same definition (lattices from
-    default_rng(seed), align-corners trilinear upsampling, weights 0.5^k,
-    min-max normalisation), upsampled on the GPU for speed; float rounding may
-    differ from value_noise in the last bits."""
+def value_noise_device(n, seed: int) -> np.ndarray:
+    """value_noise(shape, seed) (shape = n or (n, n, n)) by the same definition
+    (lattices from default_rng(seed), align-corners trilinear upsampling,
+    weights 0.5^k, min-max normalisation), upsampled on the GPU for speed;
+    float rounding may differ from value_noise in the last bits."""
     import torch
     import torch.nn.functional as F
+    shape = (n, n, n) if isinstance(n, (int, np.integer)) else tuple(int(x) for x in n)
     rng = np.random.default_rng(seed)
-    acc = torch.zeros((n, n, n), dtype=torch.float32, device="cuda")
+    acc = torch.zeros(shape, dtype=torch.float32, device="cuda")
     for k, lat in enumerate((8, 16, 32, 64)):
         v = torch.from_numpy(rng.random((lat, lat, lat), dtype=np.float32)).cuda()
-        up = F.interpolate(v[None, None], size=(n, n, n), mode="trilinear", align_corners=True)[0, 0]
+        up = F.interpolate(v[None, None], size=shape, mode="trilinear", align_corners=True)[0, 0]
         acc += (0.5 ** k) * up
     lo, hi = acc.min(), acc.max()
     return ((acc - lo) / (hi - lo)).cpu().numpy()
