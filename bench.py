@@ -63,6 +63,7 @@ def parse_args():
     # smaller cases for profiling captures
     ap.add_argument("--only", choices=["all", "plain", "serving", "diff", "batching"], default="all")
     ap.add_argument("--diff-steps", type=int, default=200, help="Adam steps of the differentiation section")
+    ap.add_argument("--no-tune", action="store_true", help="batching section: default tuning, no search")
     ap.add_argument("--storages", default=",".join(DTYPES))
     ap.add_argument("--cameras", type=int, default=16)
     ap.add_argument("--skip-cpu", action="store_true")
@@ -192,6 +193,7 @@ def pin_host_volumes(workload, torch):
 
 def serving_section(args, torch):
     from pyvr_gb300 import workloads as W
+    from pyvr_gb300.replicas import barrier
     from pyvr_gb300.server import RenderServer, SerialRenderer, drive, latency_stats, sustained_rate
     t_setup = time.perf_counter()
     wl = W.ServingWorkload(n_volumes=args.serving_volumes, n_extra=16, min_dim=128,
@@ -228,10 +230,13 @@ def serving_section(args, torch):
     server.kernel_records.clear()
     lut_misses0 = server.luts.misses
     torch.cuda.synchronize()
+    barrier()
     srv_reqs, srv_el = drive(server, wl.requests(r_server, float(args.steps), 500))
     torch.cuda.synchronize()
+    barrier()
     ser_reqs, ser_el = drive(serial, wl.requests(r_serial, float(args.steps), 600))
     torch.cuda.synchronize()
+    barrier()
     clk = clocks.stop()
     records = list(server.kernel_records)
     # roofline of the batch march kernel over the timed steps
@@ -241,12 +246,13 @@ def serving_section(args, torch):
     peak, peak_kind = measured_peaks()
     achieved = k_bytes / (k_ms / 1000.0) / 1e9 if k_ms else 0.0
     d2h = sum(r.width * r.height * 4 for r in srv_reqs)
-    # uploads: new volumes, and tables of transfer functions not yet resident
-    # (entries float4 + skip prefix int32)
-    h2d = (sum(r.volume.data.nbytes for r in srv_reqs if r.tag == "load")
-           + (server.luts.misses - lut_misses0) * (256 * 16 + 257 * 4))
+    # uploads: new volumes (tables of new transfer functions are built on the
+    # device from their control points, passed as kernel parameters)
+    h2d = sum(r.volume.data.nbytes for r in srv_reqs if r.tag == "load")
     inbox = sum(r[1] for r in records)
     out = dict(value=len(srv_reqs) / srv_el, serial_value=len(ser_reqs) / ser_el,
+               counts=(len(srv_reqs), srv_el, len(ser_reqs), ser_el),
+               lut_builds=server.luts.misses - lut_misses0,
                server=latency_stats(srv_reqs), serial=latency_stats(ser_reqs), nominal=nom,
                rate_server=r_server, rate_serial=r_serial, probes_server=probes_server,
                probes_serial=probes_serial, batches=len(records),
@@ -281,7 +287,10 @@ def batching_section(args, torch):
     from pyvr_gb300.batch import BatchRenderer, Tuning
     scenes = W.config_batching(64, noise=W.value_noise_device)
     t_tune = time.perf_counter()
-    best, results = autotune(scenes, repeats=3, use_cache=False)
+    if args.no_tune:
+        best, results = Tuning(), []
+    else:
+        best, results = autotune(scenes, repeats=3, use_cache=False)
     tune_s = time.perf_counter() - t_tune
     bench = _Bench(scenes)
     counters = torch.zeros((len(scenes), 2), dtype=torch.int64, device="cuda")
@@ -539,10 +548,12 @@ def run_ours(args):
     s = serving_section(args, torch)
     value, serial_value = s["value"], s["serial_value"]
     if world > 1:
-        # replicas: each rank serves its own stream; the job's rate is the sum
-        t = torch.tensor([value, serial_value], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t)
-        value, serial_value = t.tolist()
+        # replicas: each rank serves its own stream; the job's rate is all the
+        # ranks' completed requests over the slowest rank's time
+        from pyvr_gb300.replicas import job_rate
+        n_srv, el_srv, n_ser, el_ser = s["counts"]
+        value = job_rate(n_srv, el_srv, device="cuda")
+        serial_value = job_rate(n_ser, el_ser, device="cuda")
     cpu = None
     if rank == 0 and not args.skip_cpu:
         ct, nreq, cn, threads = cpu_serving_sample(s["workload"], args.cpu_seconds, 700)
@@ -565,7 +576,9 @@ def run_ours(args):
                 "nominal_400": s["nominal"],
                 "probes": {"server": s["probes_server"], "serial": s["probes_serial"]},
                 "batching": {"batches": s["batches"], "mean_jobs_per_batch": s["mean_batch"],
-                             "loads": s["loads"], "evictions": s["evictions"]},
+                             "loads": s["loads"], "evictions": s["evictions"],
+                             "lut_builds_timed": s["lut_builds"], "lut_hits": s["lut_hits"],
+                             "lut_misses": s["lut_misses"]},
                 "samples": {"inbox": s["inbox_samples"], "shaded": s["shaded_samples"],
                             "mean_inbox_per_request": s["mean_inbox_per_request"]},
                 "roofline": s["roofline"], "cpu_baseline": cpu, "clocks": s["clocks"],

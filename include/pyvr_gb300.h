@@ -174,6 +174,21 @@ int pvr_lut_create(const float *rgba, int size, pvr_lut **out);
 int pvr_lut_update(pvr_lut *lut, const float *rgba, int size);
 int pvr_lut_destroy(pvr_lut *lut);
 
+/* Build the LUT on the device from control points (the table
+ * set_transfer_functions makes on the host: ColorTransferFunction.to_lut /
+ * OpacityTransferFunction.to_lut, pyvr/transferfunctions/color.py:185-197,
+ * opacity.py:185-193, combined as in manager.py:162-175): entry i of each
+ * channel is numpy.interp(linspace(0, 1, size)[i], x, values) in double,
+ * rounded to float32.  Host arrays: ctf_x[n_ctf], ctf_rgb[n_ctf*3],
+ * otf_x[n_otf], otf_a[n_otf]; positions finite and sorted; 1..256 points per
+ * function; size 1..65536.  Queued on `stream` (no host synchronisation
+ * unless the table grows); no batch reading this LUT may be in flight. */
+int pvr_lut_build(pvr_lut *lut, const double *ctf_x, const double *ctf_rgb, int n_ctf,
+                  const double *otf_x, const double *otf_a, int n_otf, int size, void *stream);
+
+/* Copy the LUT (size x 4 float32) to host memory; waits for the device. */
+int pvr_lut_read(const pvr_lut *lut, float *rgba_out);
+
 /* One render of a batch: the uniforms of renderer.py:148-188, 303-316 plus
  * its resources and device output buffers. */
 typedef struct {

@@ -127,6 +127,8 @@ SIGNATURES = {
     "pvr_batch_render": (_I, [_VP, _VP, _I, _VP]),
     "pvr_batch_synchronize": (_I, [_VP]),
     "pvr_batch_render_static": (_I, [_VP, _I, _VP, _VP]),
+    "pvr_lut_build": (_I, [_VP, _VP, _VP, _I, _VP, _VP, _I, _I, _VP]),
+    "pvr_lut_read": (_I, [_VP, _VP]),
     "pvr_diff_forward": (_I, [_VP, _VP, _VP, _VP]),
     "pvr_diff_backward": (_I, [_VP, _VP, _VP, _VP, _VP, _VP, _VP]),
     "pvr_camera_spherical": (_I, [_FP, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,

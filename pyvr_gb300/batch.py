@@ -98,6 +98,34 @@ class DeviceLUT:
         self.handle = h
         self.size = int(lut.shape[0])
 
+    @classmethod
+    def on_device(cls, color_tf, opacity_tf, size: Optional[int] = None, stream=None) -> "DeviceLUT":
+        """A LUT built on the GPU from the transfer functions' control points."""
+        n = int(size or max(color_tf.lut_size, opacity_tf.lut_size))
+        lut = cls(rgba=np.zeros((n, 4), np.float32))
+        lut.build(color_tf, opacity_tf, n, stream)
+        return lut
+
+    def build(self, color_tf, opacity_tf, size: Optional[int] = None, stream=None) -> None:
+        """Rebuild the table on the GPU from control points (``pvr_lut_build``,
+        queued on ``stream``): the same float32 entries as ``rgba_lut`` computes
+        on the host.  No batch reading this LUT may be in flight."""
+        n = int(size or max(color_tf.lut_size, opacity_tf.lut_size))
+        cx = np.ascontiguousarray([float(p[0]) for p in color_tf.control_points], np.float64)
+        crgb = np.ascontiguousarray([[float(c) for c in p[1]] for p in color_tf.control_points], np.float64)
+        ox = np.ascontiguousarray([float(p[0]) for p in opacity_tf.control_points], np.float64)
+        oa = np.ascontiguousarray([float(p[1]) for p in opacity_tf.control_points], np.float64)
+        s = getattr(stream, "cuda_stream", stream)
+        check(_lib().pvr_lut_build(self.handle, cx.ctypes.data, crgb.ctypes.data, len(cx), ox.ctypes.data,
+                                   oa.ctypes.data, len(ox), n, s))
+        self.size = n
+
+    def read(self) -> np.ndarray:
+        """The table as (size, 4) float32 (waits for the device)."""
+        out = np.empty((self.size, 4), np.float32)
+        check(_lib().pvr_lut_read(self.handle, out.ctypes.data))
+        return out
+
     def update(self, rgba: np.ndarray) -> None:
         """Replace the table; no batch reading this LUT may be in flight."""
         lut = np.ascontiguousarray(rgba, dtype=np.float32)

@@ -151,24 +151,36 @@ class LutCache:
     """Device LUTs keyed by transfer-function content (``tf_key``), LRU with a
     fixed number of entries.  A LUT in use by a queued batch is pinned
     (``acquire`` / ``release``) and never rewritten; an evicted LUT's memory
-    is reused for the next new table.  Used from one thread."""
+    is reused for the next new table.  New tables are built on the GPU from
+    the control points (``DeviceLUT.build``) on the stream of the batch that
+    first needs them; ``lut.ready`` = (event, stream) lets batches on other
+    streams wait for the build.  Used from one thread."""
 
-    def __init__(self, capacity: int = 1024):
+    def __init__(self, capacity: int = 1024, device_build: bool = True):
         self.capacity = capacity
+        self.device_build = device_build
         self._luts: "collections.OrderedDict[tuple, DeviceLUT]" = collections.OrderedDict()
         self._users: Dict[tuple, int] = collections.defaultdict(int)
         self._free = _Pool(lambda n: DeviceLUT(rgba=np.zeros((n, 4), np.float32)))
         self.hits = 0
         self.misses = 0
 
-    def acquire(self, color_tf, opacity_tf):
+    def acquire(self, color_tf, opacity_tf, stream=None):
         key = tf_key(color_tf, opacity_tf)
         lut = self._luts.get(key)
         if lut is None:
-            table = rgba_lut(color_tf, opacity_tf)
             self._evict()
-            lut = self._free.get(table.shape[0])
-            lut.update(table)
+            n = max(int(color_tf.lut_size), int(opacity_tf.lut_size))
+            lut = self._free.get(n)
+            if self.device_build and stream is not None:
+                import torch
+                lut.build(color_tf, opacity_tf, n, stream)
+                ev = torch.cuda.Event()
+                ev.record(stream)
+                lut.ready = (ev, stream)
+            else:
+                lut.update(rgba_lut(color_tf, opacity_tf))
+                lut.ready = None
             self._luts[key] = lut
             self.misses += 1
         else:
@@ -378,9 +390,14 @@ class RenderServer:
         arena.reserve(total)
         base = arena.dev.data_ptr()
         cbase = self._counters[slot].data_ptr() if self.instrument else None
+        waited = set()
         for i, (req, dv) in enumerate(ready):
-            key, lut = self.luts.acquire(req.color_tf, req.opacity_tf)
+            key, lut = self.luts.acquire(req.color_tf, req.opacity_tf, stream)
             luts.append(key)
+            rd = getattr(lut, "ready", None)
+            if rd is not None and rd[1] is not stream and id(lut) not in waited:
+                stream.wait_event(rd[0])  # built on another slot's stream
+                waited.add(id(lut))
             fill_job(self._structs[i], dv.handle.value, lut.handle.value, req.camera, req.light,
                      req.config, int(req.width), int(req.height), base + offs[i], None,
                      cbase + 16 * i if cbase is not None else None)
@@ -464,7 +481,7 @@ class SerialRenderer:
             if req.volume is None:
                 raise KeyError(f"volume {req.volume_id} is not resident")
             dv = self.cache.insert(req.volume_id, req.volume, req.value_scale, self._free_now)
-        key, lut = self.luts.acquire(req.color_tf, req.opacity_tf)
+        key, lut = self.luts.acquire(req.color_tf, req.opacity_tf, self.stream)
         self.luts.release(key)  # nothing is queued after this request returns
         wh = (req.width, req.height)
         if wh not in self._bufs:
