@@ -3,28 +3,32 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-Headline ("renders/s & p50/p99 ms: batched server vs per-frame CUDA"):
-the serving workload -- a catalog of 32 HBM-resident volumes (cubic,
-extents log-uniform in 128..512, uint8 or float16 value noise, normals
-computed on the GPU) under a 40 GB budget with LRU eviction, and a seeded
-Poisson request stream mixing 70% orbit re-renders (512^2, balanced), 20% TF
-edits (512^2), 5% high-quality 1024^2 captures and 5% new-volume loads.
-For the continuously batching server and for the serial per-frame renderer
-(same resident volumes, one request at a time), an untimed sweep of offered
-rates (doubling from 400 req/s) finds the highest rate served with p99
-latency <= 20 ms; then K timed steps -- one second of the request stream
-each -- run at that rate.  value = requests completed per second by the
-server (arrival -> RGBA8 bytes in host memory: the whole path is end to end);
-the per-frame renderer's rate, the ratio and p50/p99 of both (also at the
-nominal 400 req/s) are reported beside it.  The roofline is the batch march
-kernel's (event-timed launches inside the timed steps; bytes = 8 voxel texels
-in the stored type + 8 float32x3 normal texels per shaded in-box sample).
+Headline ("renders/s & p50/p99 ms: batched server vs per-frame CUDA"): the
+serving workload.  A catalog of 32 HBM-resident volumes (cubic, extents
+log-uniform in 128..512, uint8 or float16 value noise, normals computed on
+the GPU) sits under a 40 GB budget with LRU eviction, and a seeded Poisson
+request stream mixes 70% orbit re-renders (512^2, balanced), 20% TF edits
+(512^2), 5% high-quality 1024^2 captures and 5% new-volume loads.  Both
+arms run on the native serving runtime over the same resident volumes: the
+continuously batching server, and the per-frame renderer (one request per
+launch, each read back before the next starts).  For each, an untimed sweep
+of offered rates (doubling from 400 req/s, then bisection) finds the highest
+rate served with p99 latency <= 20 ms; then K timed one-second steps run at
+that rate, backing off by 10% (at most 3 times) if the timed run misses the
+bound.  value = requests completed per second by the server, arrival ->
+RGBA8 image in host memory (the whole path is end to end); the per-frame
+rate, the ratio and p50/p99 of both (also at the nominal 400 req/s) are
+reported beside it.  The roofline is the batch march kernel's
+(event-timed launches in the timed steps; bytes = 8 voxel texels in the
+stored type + 8 float32x3 normal texels per shaded in-box sample).
 
-Nested "plain" section: the per-frame renderer on 256^3 value noise in
-u8/f16/f32, 16 orbit cameras, 1024^2, high_quality (one step = 48 frames).
+Nested sections: "plain" (the per-frame renderer on 256^3 value noise in
+u8/f16/f32, 16 orbit cameras, 1024^2, high_quality; one step = 48 frames),
+"batching_c3" (64 uneven renders per persistent launch with the autotuner's
+settings) and "differentiation" (TF recovery with the hand-written backward).
 
 --impl reference: the CPU restatement of the reference shader (the oracle,
-all host cores) serving the same request mix, on bounded row bands.
+all host cores) rendering whole frames of the same request mix.
 """
 
 import argparse
@@ -58,6 +62,8 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="oracle seconds of the CPU baseline")
     ap.add_argument("--probe-s", type=float, default=2.0, help="seconds per rate probe")
     ap.add_argument("--refine", type=int, default=3, help="bisection probes after the doubling sweep")
+    ap.add_argument("--slots", type=int, default=3, help="server: batches in flight")
+    ap.add_argument("--linger-us", type=int, default=200, help="server: hold a partial batch this long")
     ap.add_argument("--serving-volumes", type=int, default=32)
     ap.add_argument("--serving-max-dim", type=int, default=512)
     # smaller cases for profiling captures
@@ -192,19 +198,22 @@ def pin_host_volumes(workload, torch):
 
 
 def serving_section(args, torch):
+    """The batched server and the per-frame baseline, both on the native
+    serving runtime (pvr_server_*), over the same resident volumes."""
     from pyvr_gb300 import workloads as W
     from pyvr_gb300.replicas import barrier
-    from pyvr_gb300.server import RenderServer, SerialRenderer, drive, latency_stats, sustained_rate
+    from pyvr_gb300.server import NativeRenderServer, drive, latency_stats, sustained_rate
     t_setup = time.perf_counter()
     wl = W.ServingWorkload(n_volumes=args.serving_volumes, n_extra=16, min_dim=128,
                            max_dim=args.serving_max_dim, seed=0)
     pin_host_volumes(wl, torch)
-    server = RenderServer(budget_bytes=40 << 30, max_batch=64, slots=3, instrument=True)
-    serial = SerialRenderer(budget_bytes=40 << 30)
+    server = NativeRenderServer(budget_bytes=40 << 30, max_batch=64, slots=args.slots, instrument=True,
+                                linger_us=args.linger_us)
+    serial = NativeRenderServer(budget_bytes=40 << 30, per_frame=True)
     for slot in range(wl.n_catalog):
         vol, vs = wl.volumes[slot]
-        server.cache.insert(slot, vol, vs, server._release_after_inflight)
-        serial.cache.insert(slot, vol, vs, serial._free_now)
+        server.cache.insert(slot, vol, vs, server._free_volume)
+        serial.cache.insert(slot, vol, vs, serial._free_volume)
     torch.cuda.synchronize()
     setup_s = time.perf_counter() - t_setup
     # warm-up: W untimed one-second segments at the nominal rate, each impl
@@ -219,7 +228,7 @@ def serving_section(args, torch):
         st["completed_per_s"] = len(reqs) / el
         nom[name] = st
     # untimed sweep: highest rate with p99 <= 20 ms
-    rates = [NOMINAL_RATE * (2 ** k) for k in range(7)]
+    rates = [NOMINAL_RATE * (2 ** k) for k in range(8)]
     r_server, probes_server = sustained_rate(server, wl, rates, args.probe_s, 300, refine=args.refine)
     r_serial, probes_serial = sustained_rate(serial, wl, rates, args.probe_s, 400, refine=args.refine)
     r_server = r_server or NOMINAL_RATE
@@ -227,38 +236,55 @@ def serving_section(args, torch):
     # timed: K one-second steps at the sustained rate, server then serial
     clocks = ClockSampler(gpu_index(dist_env()[2]))
     clocks.start()
-    server.kernel_records.clear()
-    lut_misses0 = server.luts.misses
-    torch.cuda.synchronize()
-    barrier()
-    srv_reqs, srv_el = drive(server, wl.requests(r_server, float(args.steps), 500))
-    torch.cuda.synchronize()
-    barrier()
-    ser_reqs, ser_el = drive(serial, wl.requests(r_serial, float(args.steps), 600))
-    torch.cuda.synchronize()
-    barrier()
+    def timed_run(impl, rate, seed):
+        """K one-second steps at `rate`; a run whose p99 exceeds the bound is
+        repeated at 0.9x the rate (at most 3 times), so that the reported
+        rate is one served within the bound."""
+        attempts = []
+        for _ in range(4):
+            torch.cuda.synchronize()
+            barrier()
+            impl.reset_stats()
+            m0 = impl.luts.misses
+            reqs, el = drive(impl, wl.requests(rate, float(args.steps), seed))
+            torch.cuda.synchronize()
+            barrier()
+            lat = latency_stats(reqs)
+            attempts.append({"offered": rate, "completed_per_s": len(reqs) / el, "p99_ms": lat.get("p99_ms"),
+                             "lut_builds": impl.luts.misses - m0})
+            if lat.get("p99_ms", 1e9) <= P99_MS:
+                break
+            rate *= 0.9
+        return reqs, el, impl.stats(), attempts
+
+    srv_reqs, srv_el, st, srv_attempts = timed_run(server, r_server, 500)
+    ser_reqs, ser_el, _, ser_attempts = timed_run(serial, r_serial, 600)
     clk = clocks.stop()
-    records = list(server.kernel_records)
-    # roofline of the batch march kernel over the timed steps
-    k_ms = sum(r[0] for r in records)
-    k_bytes = sum(sh * BYTES_PER_SAMPLE["u8" if vs != 1.0 else "f16"]
-                  for r in records for (_, _, vs, sh) in r[3])
+    # our kernels in the timed region: batch marches (server), single-render
+    # marches (per-frame), LUT builds of new transfer functions (both)
+    launches = (st["batches"] + serial.stats()["batches"] + srv_attempts[-1]["lut_builds"]
+                + ser_attempts[-1]["lut_builds"])
+    r_server, r_serial = srv_attempts[-1]["offered"], ser_attempts[-1]["offered"]
+    # roofline of the batch march kernel over the timed steps: algorithmic
+    # bytes of the shaded samples / summed event-timed batch-kernel time
     peak, peak_kind = measured_peaks()
-    achieved = k_bytes / (k_ms / 1000.0) / 1e9 if k_ms else 0.0
+    k_ms = st["kernel_ms"]
+    achieved = st["algorithmic_bytes"] / (k_ms / 1000.0) / 1e9 if k_ms else 0.0
     d2h = sum(r.width * r.height * 4 for r in srv_reqs)
     # uploads: new volumes (tables of new transfer functions are built on the
     # device from their control points, passed as kernel parameters)
     h2d = sum(r.volume.data.nbytes for r in srv_reqs if r.tag == "load")
-    inbox = sum(r[1] for r in records)
     out = dict(value=len(srv_reqs) / srv_el, serial_value=len(ser_reqs) / ser_el,
                counts=(len(srv_reqs), srv_el, len(ser_reqs), ser_el),
-               lut_builds=server.luts.misses - lut_misses0,
+               lut_builds=srv_attempts[-1]["lut_builds"], launches=launches,
                server=latency_stats(srv_reqs), serial=latency_stats(ser_reqs), nominal=nom,
                rate_server=r_server, rate_serial=r_serial, probes_server=probes_server,
-               probes_serial=probes_serial, batches=len(records),
-               mean_batch=(statistics.mean(len(r[3]) for r in records) if records else 0),
-               kernel_ms=k_ms, inbox_samples=inbox, shaded_samples=sum(r[2] for r in records),
-               mean_inbox_per_request=inbox / max(1, sum(len(r[3]) for r in records)),
+               probes_serial=probes_serial, attempts={"server": srv_attempts, "serial": ser_attempts},
+               batches=st["batches"],
+               mean_batch=st["jobs"] / max(1, st["batches"]), max_batch=st["max_jobs"],
+               kernel_ms=k_ms, inbox_samples=st["inbox_samples"], shaded_samples=st["shaded_samples"],
+               mean_inbox_per_request=st["inbox_samples"] / max(1, st["jobs"]),
+               gpu_busy_frac=k_ms / 1000.0 / srv_el,
                roofline={"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
                          "kernel": "march_batch_kernel",
@@ -313,7 +339,9 @@ def batching_section(args, torch):
         for _ in range(args.warmup):
             launch()
         if count:
-            counters.zero_()
+            st.synchronize()  # the warm-up launches also add to the counters
+            with torch.cuda.stream(st):
+                counters.zero_()
             launch()
             st.synchronize()
             for j in jobs:  # count one batch only
@@ -575,7 +603,9 @@ def run_ours(args):
                 "sustained_offered": s["rate_server"],
                 "nominal_400": s["nominal"],
                 "probes": {"server": s["probes_server"], "serial": s["probes_serial"]},
+                "timed_attempts": s["attempts"],
                 "batching": {"batches": s["batches"], "mean_jobs_per_batch": s["mean_batch"],
+                             "max_jobs_per_batch": s["max_batch"], "gpu_busy_frac": s["gpu_busy_frac"],
                              "loads": s["loads"], "evictions": s["evictions"],
                              "lut_builds_timed": s["lut_builds"], "lut_hits": s["lut_hits"],
                              "lut_misses": s["lut_misses"]},
@@ -584,7 +614,7 @@ def run_ours(args):
                 "roofline": s["roofline"], "cpu_baseline": cpu, "clocks": s["clocks"],
                 "e2e": {"value": value, "unit": "renders/s", "h2d_bytes_per_step": s["h2d"],
                         "d2h_bytes_per_step": s["d2h"]},
-                "gpu_launches": s["batches"],
+                "gpu_launches": s["launches"],
                 "plain": plain, "batching_c3": batching, "differentiation": diff}
         print(json.dumps(line))
     if world > 1:

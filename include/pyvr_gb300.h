@@ -281,6 +281,78 @@ int pvr_diff_backward(const pvr_diff_scene *scene, const float *d_image, const i
                       const float *d_grad_image, float *d_grad_lut, float *d_grad_volume,
                       void *stream);
 
+/* ---- Serving runtime (no counterpart in the reference) -----------------
+ * Continuous batching of render requests over resident volumes and LUTs on
+ * native threads: a scheduler forms batches from the queued requests
+ * whenever one of `slots` launch slots (each with its own stream) is free,
+ * and a completer copies finished images to the requests' host buffers and
+ * publishes completion records.  per_frame = 1 serves one request at a time
+ * (one slot, one job per launch, the next launch after the previous image
+ * is in host memory): the per-frame baseline on the same machinery.
+ * The caller keeps each request's volume, LUT and output buffer alive until
+ * its completion has been polled. */
+typedef struct pvr_server pvr_server;
+
+enum pvr_camera_mode { PVR_CAMERA_MATRICES = 0, PVR_CAMERA_ORBIT = 1 };
+
+typedef struct {
+    pvr_volume *volume;
+    pvr_lut *lut;
+    int camera_mode;            /* PVR_CAMERA_MATRICES: view/proj/camera_pos; PVR_CAMERA_ORBIT: below */
+    float view[16], proj[16], camera_pos[3];
+    float target[3];            /* orbit camera, Camera.from_spherical fields */
+    double azimuth, elevation, roll, distance;
+    float init_pos[3], init_up[3];
+    double fov, near_plane, far_plane;
+    float light_pos[3], light_target[3];
+    float ambient, diffuse;
+    float step_size, reference_step_size;
+    int max_steps;
+    int width, height;
+    uint8_t *out_rgba8;         /* host, width*height*4 bytes, bottom row first */
+    int out_pinned;             /* 1: out_rgba8 is page-locked; the image is copied to it by DMA */
+    void *wait_event;           /* cudaEvent_t the batch must wait for (e.g. the LUT's build), or NULL */
+    unsigned long long tag;     /* echoed in the completion */
+} pvr_request;
+
+typedef struct {
+    unsigned long long tag;
+    int status;                 /* PVR_OK or the error of the batch */
+    long long t_submit_ns, t_launch_ns, t_done_ns;   /* CLOCK_MONOTONIC */
+} pvr_completion;
+
+typedef struct {
+    int max_batch;              /* requests per batch (1..4096) */
+    int slots;                  /* batches in flight (1..16) */
+    int per_frame;              /* 1: per-frame baseline */
+    int instrument;             /* 1: kernel events and sample counters per batch */
+    int linger_us;              /* with a batch in flight, hold a partial batch up to this long */
+    pvr_tuning tuning;          /* tile_w == 0: default */
+} pvr_server_config;
+
+typedef struct {
+    long long submitted, batches, jobs;
+    int max_jobs;
+    double kernel_ms;           /* summed batch-kernel event times (instrument) */
+    long long inbox_samples, shaded_samples;
+    double algorithmic_bytes;   /* shaded samples x (8 voxel + 8 x 12 normal bytes) */
+    long long queued;
+} pvr_server_stats;
+
+int pvr_server_create(const pvr_server_config *cfg, pvr_server **out);
+/* Validate and queue one request (any thread).  Orbit cameras are turned
+ * into matrices here (pvr_camera_spherical). */
+int pvr_server_submit(pvr_server *srv, const pvr_request *req);
+/* Up to `max` completions; waits up to timeout_ms for the first. */
+int pvr_server_poll(pvr_server *srv, pvr_completion *out, int max, int timeout_ms, int *n_out);
+/* paused = 1: launch nothing (submissions queue up); 0: resume. */
+int pvr_server_pause(pvr_server *srv, int paused);
+int pvr_server_get_stats(pvr_server *srv, pvr_server_stats *out);
+int pvr_server_reset_stats(pvr_server *srv);
+const char *pvr_server_last_error(pvr_server *srv);
+/* Serves every queued request, then stops the threads and frees the slots. */
+int pvr_server_destroy(pvr_server *srv);
+
 /* Orbit camera setup on the host in double precision: Camera.from_spherical
  * + get_camera_vectors / get_view_matrix / get_projection_matrix(aspect)
  * (pyvr/camera/control.py:238-351, pyvr/camera/camera.py:292-369), giving the

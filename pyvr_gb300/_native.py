@@ -127,6 +127,14 @@ SIGNATURES = {
     "pvr_batch_render": (_I, [_VP, _VP, _I, _VP]),
     "pvr_batch_synchronize": (_I, [_VP]),
     "pvr_batch_render_static": (_I, [_VP, _I, _VP, _VP]),
+    "pvr_server_create": (_I, [_VP, ctypes.POINTER(_VP)]),
+    "pvr_server_submit": (_I, [_VP, _VP]),
+    "pvr_server_poll": (_I, [_VP, _VP, _I, _I, ctypes.POINTER(_I)]),
+    "pvr_server_pause": (_I, [_VP, _I]),
+    "pvr_server_get_stats": (_I, [_VP, _VP]),
+    "pvr_server_reset_stats": (_I, [_VP]),
+    "pvr_server_last_error": (ctypes.c_char_p, [_VP]),
+    "pvr_server_destroy": (_I, [_VP]),
     "pvr_lut_build": (_I, [_VP, _VP, _VP, _I, _VP, _VP, _I, _I, _VP]),
     "pvr_lut_read": (_I, [_VP, _VP]),
     "pvr_diff_forward": (_I, [_VP, _VP, _VP, _VP]),
@@ -142,6 +150,40 @@ PVR_NORMALS_NONE, PVR_NORMALS_GIVEN, PVR_NORMALS_DEVICE = 0, 1, 2
 class PvrTuning(ctypes.Structure):
     """pvr_tuning of include/pyvr_gb300.h."""
     _fields_ = [("tile_w", _I), ("tile_h", _I), ("steps_per_iter", _I), ("blocks_per_sm", _I)]
+
+
+_D = ctypes.c_double
+PVR_CAMERA_MATRICES, PVR_CAMERA_ORBIT = 0, 1
+
+
+class PvrRequest(ctypes.Structure):
+    """pvr_request of include/pyvr_gb300.h."""
+    _fields_ = [("volume", _VP), ("lut", _VP), ("camera_mode", _I),
+                ("view", _F * 16), ("proj", _F * 16), ("camera_pos", _F * 3),
+                ("target", _F * 3), ("azimuth", _D), ("elevation", _D), ("roll", _D), ("distance", _D),
+                ("init_pos", _F * 3), ("init_up", _F * 3), ("fov", _D), ("near_plane", _D), ("far_plane", _D),
+                ("light_pos", _F * 3), ("light_target", _F * 3), ("ambient", _F), ("diffuse", _F),
+                ("step_size", _F), ("reference_step_size", _F), ("max_steps", _I),
+                ("width", _I), ("height", _I), ("out_rgba8", _VP), ("out_pinned", _I),
+                ("wait_event", _VP), ("tag", ctypes.c_ulonglong)]
+
+
+class PvrCompletion(ctypes.Structure):
+    """pvr_completion of include/pyvr_gb300.h."""
+    _fields_ = [("tag", ctypes.c_ulonglong), ("status", _I), ("t_submit_ns", _LL), ("t_launch_ns", _LL),
+                ("t_done_ns", _LL)]
+
+
+class PvrServerConfig(ctypes.Structure):
+    """pvr_server_config of include/pyvr_gb300.h."""
+    _fields_ = [("max_batch", _I), ("slots", _I), ("per_frame", _I), ("instrument", _I), ("linger_us", _I),
+                ("tuning", PvrTuning)]
+
+
+class PvrServerStats(ctypes.Structure):
+    """pvr_server_stats of include/pyvr_gb300.h."""
+    _fields_ = [("submitted", _LL), ("batches", _LL), ("jobs", _LL), ("max_jobs", _I), ("kernel_ms", _D),
+                ("inbox_samples", _LL), ("shaded_samples", _LL), ("algorithmic_bytes", _D), ("queued", _LL)]
 
 
 class PvrDiffView(ctypes.Structure):

@@ -1,0 +1,445 @@
+// Native serving runtime: continuous batching of render requests over
+// resident volumes and LUTs, with no Python on the request path.
+//
+// Threads:
+//  * submitters (any host thread): pvr_server_submit validates a request and
+//    appends it to the queue;
+//  * the scheduler: whenever a launch slot is free and requests are queued,
+//    takes up to max_batch of them (requests that arrived while other
+//    batches were on the GPU join the next batch), computes their camera
+//    matrices, and queues [batch march -> one copy of the slot's image arena
+//    to pinned host memory -> event] on the slot's stream;
+//  * the completer: waits for the slots' events in launch order, copies each
+//    image to its request's host buffer, stamps the completion time and
+//    publishes a completion record, then frees the slot.
+// Up to `slots` batches are in flight, each slot on its own stream, so one
+// batch's read-back overlaps the next batch's march.
+//
+// per_frame mode is the per-frame baseline on the same machinery: one slot,
+// one request per launch, and the next launch only after the previous
+// request's image is in host memory.
+//
+// Volumes and LUTs stay owned by the caller, who keeps each alive until the
+// completions of the requests that use it have been polled.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "pvr_internal.h"
+
+extern "C" int pvr_camera_spherical(const float target[3], double azimuth, double elevation, double roll,
+                                    double distance, const float init_pos[3], const float init_up[3],
+                                    double fov, double near_plane, double far_plane, double aspect,
+                                    float view_out[16], float proj_out[16], float pos_out[3]);
+
+namespace {
+
+long long now_ns() {
+    return std::chrono::duration_cast<std::chrono::nanoseconds>(
+               std::chrono::steady_clock::now().time_since_epoch())
+        .count();
+}
+
+struct Req {
+    pvr_request r;
+    long long t_submit;
+    long long t_launch;
+};
+
+struct Slot {
+    cudaStream_t stream = nullptr;
+    pvr_batch *batch = nullptr;
+    cudaEvent_t done = nullptr, k0 = nullptr, k1 = nullptr;
+    void *d_arena = nullptr;
+    void *h_arena = nullptr;
+    size_t cap = 0;
+    unsigned long long *d_counters = nullptr;
+    unsigned long long *h_counters = nullptr;
+    std::vector<Req> reqs;
+    std::vector<size_t> offs;
+    std::vector<pvr_job> jobs;
+    int status = PVR_OK;
+};
+
+int bytes_per_sample(int dtype) {
+    return 8 * (dtype == PVR_U8 ? 1 : dtype == PVR_F16 ? 2 : 4) + 8 * 12;
+}
+
+}  // namespace
+
+struct pvr_server {
+    pvr_server_config cfg;
+    int device = 0;
+    std::vector<Slot> slots;
+    std::mutex mu;
+    std::condition_variable cv_sched, cv_done, cv_poll;
+    std::deque<Req> queue;
+    std::deque<int> inflight;  // launched slots, in launch order
+    std::vector<int> free_slots;
+    std::deque<pvr_completion> completions;
+    bool stop = false;
+    bool paused = false;
+    bool sched_exited = false;
+    std::thread sched, completer;
+    pvr_server_stats stats;
+    std::string last_error;
+};
+
+using pvr::fail;
+
+namespace {
+
+int ensure_arena(Slot &s, size_t need) {
+    if (need <= s.cap) return PVR_OK;
+    size_t cap = 32u << 20;  // 24 images of 512^2 or 8 of 1024^2 before any growth
+    while (cap < need) cap <<= 1;
+    if (s.d_arena) PVR_CUDA(cudaFreeAsync(s.d_arena, s.stream));
+    if (s.h_arena) {
+        PVR_CUDA(cudaStreamSynchronize(s.stream));
+        cudaFreeHost(s.h_arena);
+    }
+    s.d_arena = nullptr;
+    s.h_arena = nullptr;
+    s.cap = 0;
+    PVR_CUDA(cudaMallocAsync(&s.d_arena, cap, s.stream));
+    PVR_CUDA(cudaHostAlloc(&s.h_arena, cap, cudaHostAllocPortable));
+    s.cap = cap;
+    return PVR_OK;
+}
+
+void fill_from_request(const pvr_request &r, pvr_job &j) {
+    std::memset(&j, 0, sizeof(j));
+    j.volume = r.volume;
+    j.lut = r.lut;
+    j.width = r.width;
+    j.height = r.height;
+    std::memcpy(j.view, r.view, sizeof(j.view));
+    std::memcpy(j.proj, r.proj, sizeof(j.proj));
+    std::memcpy(j.camera_pos, r.camera_pos, sizeof(j.camera_pos));
+    std::memcpy(j.light_pos, r.light_pos, sizeof(j.light_pos));
+    std::memcpy(j.light_target, r.light_target, sizeof(j.light_target));
+    j.ambient = r.ambient;
+    j.diffuse = r.diffuse;
+    j.step_size = r.step_size;
+    j.reference_step_size = r.reference_step_size;
+    j.max_steps = r.max_steps;
+}
+
+// the scheduler's half of one batch: returns the status of the launch
+int launch_slot(pvr_server *srv, Slot &s) {
+    const int n = (int)s.reqs.size();
+    s.offs.resize(n);
+    s.jobs.resize(n);
+    size_t total = 0;
+    for (int i = 0; i < n; ++i) {
+        s.offs[i] = total;
+        total += ((size_t)s.reqs[i].r.width * s.reqs[i].r.height * 4 + 255) & ~(size_t)255;
+    }
+    if (int rc = ensure_arena(s, total)) return rc;
+    for (int i = 0; i < n; ++i) {
+        void *ev = s.reqs[i].r.wait_event;
+        bool seen = false;  // one wait per distinct event
+        for (int k = 0; k < i && !seen; ++k) seen = s.reqs[k].r.wait_event == ev;
+        if (ev && !seen) PVR_CUDA(cudaStreamWaitEvent(s.stream, (cudaEvent_t)ev, 0));
+    }
+    for (int i = 0; i < n; ++i) {
+        fill_from_request(s.reqs[i].r, s.jobs[i]);
+        s.jobs[i].d_rgba8 = (char *)s.d_arena + s.offs[i];
+        s.jobs[i].d_counters = srv->cfg.instrument ? s.d_counters + 2 * i : nullptr;
+    }
+    if (srv->cfg.instrument) {
+        PVR_CUDA(cudaMemsetAsync(s.d_counters, 0, sizeof(unsigned long long) * 2 * n, s.stream));
+        PVR_CUDA(cudaEventRecord(s.k0, s.stream));
+    }
+    if (int rc = pvr_batch_render(s.batch, s.jobs.data(), n, s.stream)) return rc;
+    if (srv->cfg.instrument) {
+        PVR_CUDA(cudaEventRecord(s.k1, s.stream));
+        PVR_CUDA(cudaMemcpyAsync(s.h_counters, s.d_counters, sizeof(unsigned long long) * 2 * n,
+                                 cudaMemcpyDeviceToHost, s.stream));
+    }
+    // page-locked destinations get their image by DMA; the others through
+    // the slot's pinned arena and a host copy in the completer
+    bool staged = false;
+    for (int i = 0; i < n; ++i) {
+        const pvr_request &r = s.reqs[i].r;
+        if (r.out_pinned)
+            PVR_CUDA(cudaMemcpyAsync(r.out_rgba8, (const char *)s.d_arena + s.offs[i], (size_t)r.width * r.height * 4,
+                                     cudaMemcpyDeviceToHost, s.stream));
+        else
+            staged = true;
+    }
+    if (staged) PVR_CUDA(cudaMemcpyAsync(s.h_arena, s.d_arena, total, cudaMemcpyDeviceToHost, s.stream));
+    PVR_CUDA(cudaEventRecord(s.done, s.stream));
+    return PVR_OK;
+}
+
+void scheduler_loop(pvr_server *srv) {
+    cudaSetDevice(srv->device);
+    const long long linger_ns = (long long)srv->cfg.linger_us * 1000;
+    std::unique_lock<std::mutex> lk(srv->mu);
+    for (;;) {
+        // after stop, the queue is drained before the scheduler exits
+        if (srv->stop && srv->queue.empty()) break;
+        if ((srv->paused && !srv->stop) || srv->queue.empty() || srv->free_slots.empty()) {
+            srv->cv_sched.wait(lk);
+            continue;
+        }
+        // with a batch already on the GPU, a partial batch may wait up to
+        // linger_us (from its oldest request's submission) for more requests
+        if (!srv->cfg.per_frame && linger_ns > 0 && !srv->stop && !srv->inflight.empty() &&
+            (int)srv->queue.size() < srv->cfg.max_batch) {
+            const long long due = srv->queue.front().t_submit + linger_ns;
+            if (now_ns() < due) {
+                srv->cv_sched.wait_until(lk, std::chrono::steady_clock::time_point(std::chrono::nanoseconds(due)));
+                continue;
+            }
+        }
+        const int si = srv->free_slots.back();
+        srv->free_slots.pop_back();
+        Slot &s = srv->slots[si];
+        s.reqs.clear();
+        const int cap = srv->cfg.per_frame ? 1 : srv->cfg.max_batch;
+        while (!srv->queue.empty() && (int)s.reqs.size() < cap) {
+            s.reqs.push_back(srv->queue.front());
+            srv->queue.pop_front();
+        }
+        lk.unlock();
+        const long long t_launch = now_ns();
+        for (auto &q : s.reqs) q.t_launch = t_launch;
+        s.status = launch_slot(srv, s);
+        if (s.status != PVR_OK) {
+            const std::string why = pvr_last_error();
+            std::lock_guard<std::mutex> g(srv->mu);
+            srv->last_error = why;
+        }
+        lk.lock();
+        srv->inflight.push_back(si);
+        srv->cv_done.notify_one();
+    }
+    srv->sched_exited = true;
+    srv->cv_done.notify_all();
+}
+
+void completer_loop(pvr_server *srv) {
+    cudaSetDevice(srv->device);
+    std::unique_lock<std::mutex> lk(srv->mu);
+    for (;;) {
+        srv->cv_done.wait(lk, [&] { return !srv->inflight.empty() || srv->sched_exited; });
+        if (srv->inflight.empty()) {
+            if (srv->sched_exited) break;
+            continue;
+        }
+        const int si = srv->inflight.front();
+        lk.unlock();
+        Slot &s = srv->slots[si];
+        int status = s.status;
+        if (status == PVR_OK) {
+            const cudaError_t e = cudaEventSynchronize(s.done);
+            if (e != cudaSuccess) status = pvr::cuda_fail(e, "batch completion");
+        }
+        const long long t_done = now_ns();
+        std::vector<pvr_completion> out(s.reqs.size());
+        long long inbox = 0, shaded = 0;
+        double alg = 0.0;
+        float kms = 0.0f;
+        for (size_t i = 0; i < s.reqs.size(); ++i) {
+            const pvr_request &r = s.reqs[i].r;
+            if (status == PVR_OK && !r.out_pinned)
+                std::memcpy(r.out_rgba8, (const char *)s.h_arena + s.offs[i], (size_t)r.width * r.height * 4);
+            out[i].tag = r.tag;
+            out[i].status = status;
+            out[i].t_submit_ns = s.reqs[i].t_submit;
+            out[i].t_launch_ns = s.reqs[i].t_launch;
+            out[i].t_done_ns = t_done;
+            if (status == PVR_OK && srv->cfg.instrument) {
+                inbox += (long long)s.h_counters[2 * i];
+                shaded += (long long)s.h_counters[2 * i + 1];
+                alg += (double)s.h_counters[2 * i + 1] * bytes_per_sample(r.volume->dtype);
+            }
+        }
+        if (status == PVR_OK && srv->cfg.instrument) cudaEventElapsedTime(&kms, s.k0, s.k1);
+        lk.lock();
+        srv->stats.batches += 1;
+        srv->stats.jobs += (long long)s.reqs.size();
+        srv->stats.max_jobs = std::max(srv->stats.max_jobs, (int)s.reqs.size());
+        srv->stats.kernel_ms += kms;
+        srv->stats.inbox_samples += inbox;
+        srv->stats.shaded_samples += shaded;
+        srv->stats.algorithmic_bytes += alg;
+        for (auto &c : out) srv->completions.push_back(c);
+        s.reqs.clear();
+        srv->inflight.pop_front();
+        srv->free_slots.push_back(si);
+        srv->cv_sched.notify_one();
+        srv->cv_poll.notify_all();
+    }
+}
+
+void destroy_slots(pvr_server *srv) {
+    for (auto &s : srv->slots) {
+        if (s.stream) cudaStreamSynchronize(s.stream);
+        if (s.batch) pvr_batch_destroy(s.batch);
+        if (s.d_arena) cudaFree(s.d_arena);
+        if (s.h_arena) cudaFreeHost(s.h_arena);
+        if (s.d_counters) cudaFree(s.d_counters);
+        if (s.h_counters) cudaFreeHost(s.h_counters);
+        if (s.done) cudaEventDestroy(s.done);
+        if (s.k0) cudaEventDestroy(s.k0);
+        if (s.k1) cudaEventDestroy(s.k1);
+        if (s.stream) cudaStreamDestroy(s.stream);
+        s = Slot();
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int pvr_server_create(const pvr_server_config *cfg, pvr_server **out) {
+    if (!cfg || !out) return fail(PVR_ERR_VALUE, "NULL argument");
+    *out = nullptr;
+    if (cfg->max_batch < 1 || cfg->max_batch > 4096) return fail(PVR_ERR_VALUE, "max_batch must be in 1..4096");
+    if (cfg->slots < 1 || cfg->slots > 16) return fail(PVR_ERR_VALUE, "slots must be in 1..16");
+    pvr_server *srv = new pvr_server();
+    srv->cfg = *cfg;
+    if (srv->cfg.per_frame) {
+        srv->cfg.slots = 1;
+        srv->cfg.max_batch = 1;
+    }
+    std::memset(&srv->stats, 0, sizeof(srv->stats));
+    cudaGetDevice(&srv->device);
+    srv->slots.resize(srv->cfg.slots);
+    int rc = PVR_OK;
+    for (auto &s : srv->slots) {
+        cudaError_t e = cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreate(&s.k0);
+        if (e == cudaSuccess) e = cudaEventCreate(&s.k1);
+        if (e == cudaSuccess)
+            e = cudaMalloc(&s.d_counters, sizeof(unsigned long long) * 2 * srv->cfg.max_batch);
+        if (e == cudaSuccess)
+            e = cudaHostAlloc(&s.h_counters, sizeof(unsigned long long) * 2 * srv->cfg.max_batch,
+                              cudaHostAllocPortable);
+        if (e != cudaSuccess) {
+            rc = pvr::cuda_fail(e, "pvr_server_create");
+            break;
+        }
+        if ((rc = pvr_batch_create(srv->cfg.max_batch, 1, &s.batch))) break;
+        if (cfg->tuning.tile_w && (rc = pvr_batch_set_tuning(s.batch, &cfg->tuning))) break;
+    }
+    if (rc != PVR_OK) {
+        destroy_slots(srv);
+        delete srv;
+        return rc;
+    }
+    for (int i = srv->cfg.slots - 1; i >= 0; --i) srv->free_slots.push_back(i);
+    srv->sched = std::thread(scheduler_loop, srv);
+    srv->completer = std::thread(completer_loop, srv);
+    *out = srv;
+    return PVR_OK;
+}
+
+int pvr_server_submit(pvr_server *srv, const pvr_request *req) {
+    if (!srv || !req) return fail(PVR_ERR_VALUE, "NULL argument");
+    const pvr_request &r = *req;
+    if (!r.volume || !r.lut) return fail(PVR_ERR_VALUE, "request without volume or LUT");
+    if (!r.volume->layout_ready) return fail(PVR_ERR_STATE, "volume layout not built");
+    if (!r.out_rgba8) return fail(PVR_ERR_VALUE, "request without output buffer");
+    if (r.width <= 0 || r.height <= 0 || r.width > 32768 || r.height > 32768)
+        return fail(PVR_ERR_VALUE, "request size must be in 1..32768, got %dx%d", r.width, r.height);
+    if (!(r.step_size > 0.0f) || !(r.reference_step_size > 0.0f) || r.max_steps < 1)
+        return fail(PVR_ERR_VALUE, "invalid step_size / reference_step_size / max_steps");
+    Req q;
+    q.r = r;
+    if (r.camera_mode == PVR_CAMERA_ORBIT) {
+        if (int rc = pvr_camera_spherical(r.target, r.azimuth, r.elevation, r.roll, r.distance, r.init_pos,
+                                          r.init_up, r.fov, r.near_plane, r.far_plane,
+                                          (double)r.width / (double)r.height, q.r.view, q.r.proj,
+                                          q.r.camera_pos))
+            return rc;
+    } else if (r.camera_mode != PVR_CAMERA_MATRICES) {
+        return fail(PVR_ERR_VALUE, "unknown camera_mode %d", r.camera_mode);
+    }
+    q.t_submit = now_ns();
+    {
+        std::lock_guard<std::mutex> g(srv->mu);
+        if (srv->stop) return fail(PVR_ERR_STATE, "server is shutting down");
+        srv->queue.push_back(q);
+        srv->stats.submitted += 1;
+    }
+    srv->cv_sched.notify_one();
+    return PVR_OK;
+}
+
+int pvr_server_poll(pvr_server *srv, pvr_completion *out, int max, int timeout_ms, int *n_out) {
+    if (!srv || !out || !n_out || max < 1) return fail(PVR_ERR_VALUE, "invalid poll arguments");
+    *n_out = 0;
+    std::unique_lock<std::mutex> lk(srv->mu);
+    if (srv->completions.empty() && timeout_ms > 0)
+        srv->cv_poll.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] { return !srv->completions.empty(); });
+    int n = 0;
+    while (n < max && !srv->completions.empty()) {
+        out[n++] = srv->completions.front();
+        srv->completions.pop_front();
+    }
+    *n_out = n;
+    return PVR_OK;
+}
+
+int pvr_server_pause(pvr_server *srv, int paused) {
+    if (!srv) return fail(PVR_ERR_VALUE, "NULL argument");
+    {
+        std::lock_guard<std::mutex> g(srv->mu);
+        srv->paused = paused != 0;
+    }
+    srv->cv_sched.notify_all();
+    return PVR_OK;
+}
+
+int pvr_server_get_stats(pvr_server *srv, pvr_server_stats *out) {
+    if (!srv || !out) return fail(PVR_ERR_VALUE, "NULL argument");
+    std::lock_guard<std::mutex> g(srv->mu);
+    *out = srv->stats;
+    out->queued = (long long)srv->queue.size();
+    return PVR_OK;
+}
+
+int pvr_server_reset_stats(pvr_server *srv) {
+    if (!srv) return fail(PVR_ERR_VALUE, "NULL argument");
+    std::lock_guard<std::mutex> g(srv->mu);
+    std::memset(&srv->stats, 0, sizeof(srv->stats));
+    return PVR_OK;
+}
+
+const char *pvr_server_last_error(pvr_server *srv) {
+    if (!srv) return "null server";
+    std::lock_guard<std::mutex> g(srv->mu);
+    thread_local std::string copy;
+    copy = srv->last_error;
+    return copy.c_str();
+}
+
+int pvr_server_destroy(pvr_server *srv) {
+    if (!srv) return PVR_OK;
+    {
+        std::lock_guard<std::mutex> g(srv->mu);
+        srv->stop = true;
+    }
+    // the scheduler drains the queue before it exits; the completer drains
+    // the launched slots
+    srv->cv_sched.notify_all();
+    if (srv->sched.joinable()) srv->sched.join();
+    srv->cv_done.notify_all();
+    if (srv->completer.joinable()) srv->completer.join();
+    destroy_slots(srv);
+    delete srv;
+    return PVR_OK;
+}
+
+}  // extern "C"

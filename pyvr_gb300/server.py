@@ -29,9 +29,11 @@ request at a time, each rendered and read back before the next starts.
 from __future__ import annotations
 
 import collections
+import ctypes
 import queue
 import threading
 import time
+import weakref
 from concurrent.futures import Future
 from dataclasses import dataclass, field
 from typing import Dict, List, Optional
@@ -64,6 +66,7 @@ class RenderRequest:
     tag: str = ""
     future: Future = field(default_factory=Future)
     done_at: float = 0.0
+    launched_at: float = 0.0
 
 
 class VolumeCache:
@@ -141,10 +144,18 @@ class VolumeCache:
 
 def tf_key(color_tf, opacity_tf) -> tuple:
     """Content key of a transfer-function pair: equal keys give equal tables
-    (``rgba_lut`` depends on the control points and LUT sizes alone)."""
-    return (tuple((float(x), tuple(float(c) for c in rgb)) for x, rgb in color_tf.control_points),
-            tuple((float(x), float(a)) for x, a in opacity_tf.control_points),
-            int(color_tf.lut_size), int(opacity_tf.lut_size))
+    (``rgba_lut`` depends on the control points and LUT sizes alone).  Control
+    points held as tuples of numbers are keyed as they are; anything else
+    (lists, arrays) is normalised to tuples of floats first."""
+    key = (tuple(color_tf.control_points), tuple(opacity_tf.control_points),
+           color_tf.lut_size, opacity_tf.lut_size)
+    try:
+        hash(key)
+        return key
+    except TypeError:
+        return (tuple((float(x), tuple(float(c) for c in rgb)) for x, rgb in color_tf.control_points),
+                tuple((float(x), float(a)) for x, a in opacity_tf.control_points),
+                int(color_tf.lut_size), int(opacity_tf.lut_size))
 
 
 class LutCache:
@@ -165,7 +176,9 @@ class LutCache:
         self.hits = 0
         self.misses = 0
 
-    def acquire(self, color_tf, opacity_tf, stream=None):
+    def acquire(self, color_tf, opacity_tf, stream=None, sync: bool = False):
+        """(key, DeviceLUT) of the pair, built if new; pinned until release(key).
+        sync: wait for a new table's build before returning."""
         key = tf_key(color_tf, opacity_tf)
         lut = self._luts.get(key)
         if lut is None:
@@ -175,9 +188,15 @@ class LutCache:
             if self.device_build and stream is not None:
                 import torch
                 lut.build(color_tf, opacity_tf, n, stream)
-                ev = torch.cuda.Event()
-                ev.record(stream)
-                lut.ready = (ev, stream)
+                if sync:
+                    stream.synchronize()
+                    lut.ready = None
+                else:
+                    ev = getattr(lut, "_event", None)
+                    if ev is None:
+                        ev = lut._event = torch.cuda.Event()
+                    ev.record(stream)
+                    lut.ready = (ev, stream)
             else:
                 lut.update(rgba_lut(color_tf, opacity_tf))
                 lut.ready = None
@@ -501,6 +520,239 @@ class SerialRenderer:
         self.launcher.close()
 
 
+class _PinnedPool:
+    """Page-locked result buffers carved from one pinned block and recycled:
+    a result array hands its slab back when it is garbage-collected.
+    Bounded: once the block is used up, results go to ordinary memory."""
+
+    def __init__(self, torch, cap_bytes: int = 1 << 30):
+        self._block = torch.empty(cap_bytes, dtype=torch.uint8).pin_memory()
+        self._np = self._block.numpy()
+        self._base = self._block.data_ptr()
+        self._top = 0
+        self._cap = cap_bytes
+        self._free = collections.defaultdict(list)  # slab size -> offsets
+        self._lock = threading.Lock()
+
+    def get(self, n: int) -> Optional[int]:
+        """Offset of a free slab of n bytes (256-byte aligned), or None."""
+        with self._lock:
+            lst = self._free[n]
+            if lst:
+                return lst.pop()
+            size = (n + 255) & ~255
+            if self._top + size > self._cap:
+                return None
+            off = self._top
+            self._top += size
+            return off
+
+    def put(self, n: int, off: int) -> None:
+        with self._lock:
+            self._free[n].append(off)
+
+    def address(self, off: int) -> int:
+        return self._base + off
+
+    def wrap(self, n: int, off: int) -> np.ndarray:
+        """The slab as a numpy array that hands the slab back when it dies."""
+        arr = self._np[off:off + n]
+        weakref.finalize(arr, self.put, n, off)
+        return arr
+
+
+class NativeRenderServer:
+    """Continuous-batching render server on the native runtime
+    (``pvr_server_*``): batch formation, launches, read-back and completion
+    run on C++ threads; Python resolves residency (volumes, LUTs) at submit
+    and hands results back.
+
+    A result is the request's RGBA8 image as a flat uint8 array (H*W*4,
+    bottom row first: the bytes ``render()`` returns).  per_frame=True is
+    the per-frame baseline on the same runtime (one request per launch, each
+    read back before the next starts)."""
+
+    def __init__(self, budget_bytes: int = 40 << 30, max_batch: int = 64, slots: int = 3,
+                 tuning: Optional[Tuning] = None, brick_log2: int = 3, loaders: int = 2,
+                 instrument: bool = False, per_frame: bool = False, linger_us: int = 0):
+        import torch
+        self.torch = torch
+        self.cache = VolumeCache(budget_bytes, brick_log2)
+        self.luts = LutCache()
+        self.per_frame = per_frame
+        self._lut_stream = torch.cuda.Stream()
+        self._release_stream = torch.cuda.Stream()
+        self._lock = threading.Lock()  # LUT cache and in-flight table
+        self._pool = _PinnedPool(torch)
+        self._lib = _native.load()
+        cfg = _native.PvrServerConfig(int(max_batch), int(slots), int(per_frame), int(instrument),
+                                      int(linger_us),
+                                      tuning.c() if tuning is not None else _native.PvrTuning(0, 0, 0, 0))
+        h = ctypes.c_void_p()
+        _native.check(self._lib.pvr_server_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self._h = h
+        self._inflight: Dict[int, tuple] = {}
+        self._next_tag = 1
+        self._loads: "queue.Queue[RenderRequest]" = queue.Queue()
+        self._stop = False
+        self._threads = [threading.Thread(target=self._poll_loop, daemon=True, name="pvr-poll")]
+        self._threads += [threading.Thread(target=self._load_loop, daemon=True, name=f"pvr-load{i}")
+                          for i in range(loaders)]
+        for t in self._threads:
+            t.start()
+
+    # -- client API -------------------------------------------------------------
+    def submit(self, req: RenderRequest) -> Future:
+        if not req.arrival:
+            req.arrival = time.perf_counter()
+        if req.kind == "load":
+            self._loads.put(req)
+        else:
+            self._submit_render(req)
+        return req.future
+
+    def pause(self, paused: bool = True) -> None:
+        """Hold launches (submissions queue up) or resume them."""
+        _native.check(self._lib.pvr_server_pause(self._h, int(paused)))
+
+    def stats(self) -> dict:
+        st = _native.PvrServerStats()
+        _native.check(self._lib.pvr_server_get_stats(self._h, ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in st._fields_}
+
+    def reset_stats(self) -> None:
+        _native.check(self._lib.pvr_server_reset_stats(self._h))
+
+    def close(self) -> None:
+        if self._h is None:
+            return
+        deadline = time.time() + 120
+        while self._inflight and time.time() < deadline:
+            time.sleep(0.001)
+        self._stop = True
+        for _ in self._threads:
+            self._loads.put(None)
+        for t in self._threads:  # the poller exits once nothing is in flight
+            t.join(timeout=30)
+        h, self._h = self._h, None
+        self._lib.pvr_server_destroy(h)
+        self.torch.cuda.synchronize()
+
+    # -- internals -----------------------------------------------------------------
+    def _free_volume(self, dv: DeviceVolume) -> None:
+        """An evicted volume: no request uses it any more (every batch that read
+        it has completed), so it is freed in the order of a private stream."""
+        _native.check(self._lib.pvr_volume_release(dv.handle, self._release_stream.cuda_stream))
+        dv.handle = None
+
+    def _load_loop(self) -> None:
+        self.torch.cuda.set_device(self.torch.cuda.current_device())
+        while True:
+            req = self._loads.get()
+            if req is None or self._stop:
+                return
+            try:
+                self.cache.insert(req.volume_id, req.volume, req.value_scale, self._free_volume)
+            except Exception as e:
+                req.future.set_exception(e)
+                continue
+            req.kind = "render"
+            self._submit_render(req)
+
+    def _submit_render(self, req: RenderRequest) -> None:
+        dv = self.cache.acquire(req.volume_id)
+        if dv is None:  # not resident (evicted meanwhile): load it, then render
+            if req.volume is None:
+                req.future.set_exception(KeyError(f"volume {req.volume_id} is not resident"))
+            else:
+                req.kind = "load"
+                self._loads.put(req)
+            return
+        key = tag = out = None
+        try:
+            with self._lock:
+                key, lut = self.luts.acquire(req.color_tf, req.opacity_tf, self._lut_stream)
+                tag = self._next_tag
+                self._next_tag += 1
+            nbytes = req.width * req.height * 4
+            slab = self._pool.get(nbytes) if nbytes > 0 else None
+            out = (nbytes, slab) if slab is not None else np.empty(nbytes, np.uint8)
+            r = _native.PvrRequest()
+            r.camera_mode = _native.PVR_CAMERA_ORBIT
+            r.volume = dv.handle.value
+            r.lut = lut.handle.value
+            rd = getattr(lut, "ready", None)
+            r.wait_event = rd[0].cuda_event if rd is not None else None
+            cam = req.camera
+            t, ip, iu = cam.target, cam.init_pos, cam.init_up
+            r.target[0], r.target[1], r.target[2] = float(t[0]), float(t[1]), float(t[2])
+            r.init_pos[0], r.init_pos[1], r.init_pos[2] = float(ip[0]), float(ip[1]), float(ip[2])
+            r.init_up[0], r.init_up[1], r.init_up[2] = float(iu[0]), float(iu[1]), float(iu[2])
+            r.azimuth, r.elevation, r.roll = float(cam.azimuth), float(cam.elevation), float(cam.roll)
+            r.distance, r.fov = float(cam.distance), float(cam.fov)
+            r.near_plane, r.far_plane = float(cam.near_plane), float(cam.far_plane)
+            lp, lt, light = req.light.position, req.light.target, req.light
+            r.light_pos[0], r.light_pos[1], r.light_pos[2] = float(lp[0]), float(lp[1]), float(lp[2])
+            r.light_target[0], r.light_target[1], r.light_target[2] = float(lt[0]), float(lt[1]), float(lt[2])
+            r.ambient, r.diffuse = float(light.ambient_intensity), float(light.diffuse_intensity)
+            cfg = req.config
+            r.step_size, r.reference_step_size = float(cfg.step_size), float(cfg.reference_step_size)
+            r.max_steps = int(cfg.max_steps)
+            r.width, r.height = int(req.width), int(req.height)
+            r.out_rgba8 = self._pool.address(slab) if slab is not None else out.ctypes.data
+            r.out_pinned = int(slab is not None)
+            r.tag = tag
+            self._inflight[tag] = (req, req.volume_id, key, out)
+            rc = self._lib.pvr_server_submit(self._h, ctypes.byref(r))
+            if rc == _native.PVR_ERR_VALUE and b"parallel" in self._lib.pvr_last_error():
+                # degenerate orbit camera: the Camera methods' matrices
+                from .renderer import camera_uniforms
+                v, p, c = camera_uniforms(cam, req.width, req.height)
+                r.camera_mode = _native.PVR_CAMERA_MATRICES
+                r.view[:] = v.ravel().tolist()
+                r.proj[:] = p.ravel().tolist()
+                r.camera_pos[:] = c.tolist()
+                rc = self._lib.pvr_server_submit(self._h, ctypes.byref(r))
+            _native.check(rc)
+        except Exception as e:
+            self._inflight.pop(tag, None)
+            if isinstance(out, tuple):
+                self._pool.put(*out)
+            self.cache.release(req.volume_id)
+            if key is not None:
+                with self._lock:
+                    self.luts.release(key)
+            req.future.set_exception(e)
+
+    def _poll_loop(self) -> None:
+        comps = (_native.PvrCompletion * 256)()
+        n = ctypes.c_int(0)
+        h = self._h
+        while True:
+            if self._lib.pvr_server_poll(h, comps, 256, 20, ctypes.byref(n)) != 0:
+                return
+            for c in comps[:n.value]:
+                req, vid, key, out = self._inflight.pop(c.tag)
+                self.cache.release(vid)
+                with self._lock:
+                    self.luts.release(key)
+                req.done_at = c.t_done_ns / 1e9
+                req.launched_at = c.t_launch_ns / 1e9
+                if not isinstance(out, np.ndarray):
+                    if c.status == 0:
+                        out = self._pool.wrap(*out)
+                    else:
+                        self._pool.put(*out)
+                if c.status == 0:
+                    req.future.set_result(out)
+                else:
+                    req.future.set_exception(RuntimeError(
+                        f"render failed (status {c.status}): "
+                        f"{self._lib.pvr_server_last_error(self._h).decode(errors='replace')}"))
+            if self._stop and not self._inflight:
+                return
+
+
 def latency_stats(reqs: List[RenderRequest]) -> dict:
     lat = np.array([(r.done_at - r.arrival) * 1000.0 for r in reqs if r.done_at])
     if lat.size == 0:
@@ -518,20 +770,34 @@ def _wait_until(t: float) -> None:
         time.sleep(dt - 0.0003 if dt > 0.0006 else 0.00005)
 
 
+_CONSUMED: Future = Future()
+_CONSUMED.set_result(None)
+
+
+def _consume(req: RenderRequest):
+    """Done-callback of a load-generating client: the image is taken and
+    dropped at once (its buffer can be reused), the timings stay."""
+    def cb(f):
+        if f.exception() is None:
+            req.future = _CONSUMED
+    return cb
+
+
 def drive(impl, stream, timeout: float = 300.0):
     """Replay a request stream [(arrival offset s, RenderRequest kwargs)] in
-    real time against a RenderServer or a SerialRenderer (open loop: a client
-    thread submits at the arrival times whatever the service does).  Returns
-    (requests, seconds from the first arrival to the last completion)."""
+    real time against a server or a SerialRenderer (open loop: a client
+    thread submits at the arrival times whatever the service does, and drops
+    each image as soon as it arrives).  Returns (requests, seconds from the
+    first arrival to the last completion)."""
     reqs = [RenderRequest(**kw) for _, kw in stream]
     if not reqs:
         return reqs, 0.0
-    if isinstance(impl, RenderServer):
+    if not isinstance(impl, SerialRenderer):
         t0 = time.perf_counter()
         for (off, _), req in zip(stream, reqs):
             _wait_until(t0 + off)
             req.arrival = time.perf_counter()
-            impl.submit(req)
+            impl.submit(req).add_done_callback(_consume(req))
         for req in reqs:
             req.future.result(timeout=timeout)
         return reqs, max(r.done_at for r in reqs) - t0

@@ -68,3 +68,64 @@ def test_server_with_evictions():
     for g, w in zip(got, want):
         assert g == w
     assert stats["evictions"] > 0
+
+
+def _run_native(budget, n_req=160, per_frame=False, max_batch=16):
+    """Results of the native server (batched or per-frame) and of the serial
+    Python renderer for the same stream."""
+    from pyvr_gb300.server import NativeRenderServer
+    wl = _workload()
+    stream = wl.requests(rate=4000.0, duration=1.0, seed=3)[:n_req]
+    server = NativeRenderServer(budget_bytes=budget, max_batch=max_batch, slots=3, per_frame=per_frame,
+                                instrument=True)
+    serial = SerialRenderer()
+    for slot in range(wl.n_catalog):
+        vol, vs = wl.volumes[slot]
+        server.cache.insert(slot, vol, vs, server._free_volume)
+        serial.cache.insert(slot, vol, vs, serial._free_now)
+    reqs = [RenderRequest(**kw) for _, kw in stream]
+    # the first half is held and released at once (full batches), the second
+    # half is served as it arrives
+    server.pause(True)
+    futs = [server.submit(r) for r in reqs[:n_req // 2]]
+    server.pause(False)
+    futs += [server.submit(r) for r in reqs[n_req // 2:]]
+    got = [f.result(timeout=120) for f in futs]
+    want = [serial.handle(RenderRequest(**kw)) for _, kw in stream]
+    stats = server.stats()
+    stats.update(evictions=server.cache.evictions, lat=latency_stats(reqs))
+    server.close()
+    serial.close()
+    return wl, stream, got, want, stats
+
+
+@pytest.mark.parametrize("per_frame", [False, True])
+def test_native_server_results_equal_results_alone(per_frame):
+    wl, stream, got, want, stats = _run_native(budget=40 << 30, per_frame=per_frame)
+    for (_, kw), g, w in zip(stream, got, want):
+        assert g.dtype == np.uint8 and g.size == kw["width"] * kw["height"] * 4
+        assert g.tobytes() == w
+    assert stats["jobs"] == len(stream) and stats["shaded_samples"] > 0
+    if per_frame:
+        assert stats["max_jobs"] == 1 and stats["batches"] == len(stream)
+    else:
+        assert stats["max_jobs"] == 16  # held requests formed full batches
+    assert stats["lat"]["n"] == len(stream)
+
+
+def test_native_server_with_evictions_and_bad_requests():
+    wl, stream, got, want, stats = _run_native(budget=3 << 20, n_req=120)
+    for g, w in zip(got, want):
+        assert g.tobytes() == w
+    assert stats["evictions"] > 0
+    from pyvr_gb300.server import NativeRenderServer
+    server = NativeRenderServer(budget_bytes=1 << 30)
+    vol, vs = wl.volumes[0]
+    server.cache.insert(0, vol, vs, server._free_volume)
+    kw = dict(stream[0][1], volume_id=0, width=0, kind="render")
+    with pytest.raises(ValueError, match="size"):
+        server.submit(RenderRequest(**kw)).result(timeout=30)
+    kw = dict(stream[0][1], volume_id=99, kind="render", volume=None)
+    with pytest.raises(KeyError):
+        server.submit(RenderRequest(**kw)).result(timeout=30)
+    server.close()
