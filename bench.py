@@ -50,6 +50,12 @@ DTYPES = ("u8", "f16", "f32")
 RES = 1024
 N_VOL = 256
 NOMINAL_RATE = 400.0
+# DRAM bytes per in-box sample of the batch march kernel on the serving mix
+# (ncu, 3 launches of a 4-volume serving case: 98.8 MB for about 32.7 M
+# samples) and DRAM bytes of one 1024^2 high_quality f32 frame of the plain
+# workload (ncu, one launch): the traffic estimates of the roofline entries
+SERVING_DRAM_BYTES_PER_SAMPLE = 3.0
+PLAIN_F32_DRAM_BYTES_PER_FRAME = 100.4e6
 P99_MS = 20.0
 
 
@@ -66,6 +72,7 @@ def parse_args():
     ap.add_argument("--linger-us", type=int, default=200, help="server: hold a partial batch this long")
     ap.add_argument("--serving-volumes", type=int, default=32)
     ap.add_argument("--serving-max-dim", type=int, default=512)
+    ap.add_argument("--serving-extra", type=int, default=16, help="volumes outside the catalog (loads)")
     # smaller cases for profiling captures
     ap.add_argument("--only", choices=["all", "plain", "serving", "diff", "batching"], default="all")
     ap.add_argument("--diff-steps", type=int, default=200, help="Adam steps of the differentiation section")
@@ -204,7 +211,7 @@ def serving_section(args, torch):
     from pyvr_gb300.replicas import barrier
     from pyvr_gb300.server import NativeRenderServer, drive, latency_stats, sustained_rate
     t_setup = time.perf_counter()
-    wl = W.ServingWorkload(n_volumes=args.serving_volumes, n_extra=16, min_dim=128,
+    wl = W.ServingWorkload(n_volumes=args.serving_volumes, n_extra=args.serving_extra, min_dim=128,
                            max_dim=args.serving_max_dim, seed=0)
     pin_host_volumes(wl, torch)
     server = NativeRenderServer(budget_bytes=40 << 30, max_batch=64, slots=args.slots, instrument=True,
@@ -286,7 +293,10 @@ def serving_section(args, torch):
                mean_inbox_per_request=st["inbox_samples"] / max(1, st["jobs"]),
                gpu_busy_frac=k_ms / 1000.0 / srv_el,
                roofline={"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                         "frac": achieved / peak, "peak_kind": peak_kind,
+                         "traffic": SERVING_DRAM_BYTES_PER_SAMPLE * st["shaded_samples"] / max(1, st["batches"]),
+                         "traffic_note": "per launch, scaled from a reduced-catalog ncu capture by samples",
+                         "algorithmic_bytes_per_launch": st["algorithmic_bytes"] / max(1, st["batches"]),
                          "kernel": "march_batch_kernel",
                          "note": "batches in flight on different streams may overlap; summed launch "
                                  "times make this a lower bound"},
@@ -537,6 +547,8 @@ def plain_section(args, torch):
             "samples_per_s": sum(samples[(dt, k)] for dt, k, _ in launch_ms) / elapsed,
             "roofline": {"bound": "hbm", "achieved": tot_bytes / tot_s / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": tot_bytes / tot_s / 1e9 / peak, "peak_kind": peak_kind,
+                         "traffic": PLAIN_F32_DRAM_BYTES_PER_FRAME if "f32" in rend else None,
+                         "traffic_note": "f32 frame, one full-size ncu launch",
                          "kernel": "march_single_kernel", "per_storage": per_dtype},
             "gpu_launches": len(launch_ms),
             "config": {"volume": f"{N_VOL}^3 value noise seed 0", "storages": list(rend),
