@@ -113,7 +113,9 @@ __device__ __forceinline__ void shade_sample(const MarchFrame &f, const float4 *
     const float la = __fadd_rn(lu, -lfl);
     const float lmax = (float)(f.lut_size - 1);
     const int i0 = lut_index(lfl, lmax, f.lut_size);
-    const int i1 = lut_index(__fadd_rn(lfl, 1.0f), lmax, f.lut_size);
+    // = lut_index(lfl + 1): the next entry from lfl >= 0 on, clamped to the
+    // table (NaN and negative coordinates stay on entry 0)
+    const int i1 = min(i0 + (lfl >= 0.0f ? 1 : 0), f.lut_size - 1);
     const float4 A = lut_entry<SMEM_LUT>(lut, i0), B = lut_entry<SMEM_LUT>(lut, i1);
     const float2 crg = lerp_tex2(lo2(A), lo2(B), la);
     const float2 cba = lerp_tex2(hi2(A), hi2(B), la);  // (blue, alpha_tf)

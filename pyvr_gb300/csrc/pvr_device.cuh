@@ -66,10 +66,11 @@ __device__ __forceinline__ float pvr_expf(float x) {
     p = fmaf(p, r, 0.5f);
     p = fmaf(p, r, 1.0f);
     p = fmaf(p, r, 1.0f);
-    int k = (int)kf;
-    int k1 = k > 0 ? k / 2 : 0;
-    int k2 = k - k1;
-    return (p * __int_as_float((k1 + 127) << 23)) * __int_as_float((k2 + 127) << 23);
+    const int k = (int)kf;  // -126 .. 128
+    // one exact scaling by 2^k where 2^k is a float (k <= 127); k = 128 in
+    // two halves.  Either way the only rounding is that of the final product.
+    if (k <= 127) return p * __int_as_float((k + 127) << 23);
+    return (p * __int_as_float((64 + 127) << 23)) * __int_as_float((k - 64 + 127) << 23);
 }
 
 // Ray of pixel (px, py), py counted from the bottom row: vertex-stage uv at

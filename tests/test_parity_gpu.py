@@ -246,3 +246,60 @@ def test_lut_change_recomputes_skip_flags():
     assert sh0 < in0          # the sparse LUT leaves transparent bricks to skip
     assert sh1 == in1         # alpha >= 0.02 everywhere: nothing is skipped
     assert outs[2][3] == outs[0][3]
+
+
+def _check_nan_equal(vol, cam, light, cfg, ctf, otf, w, h, **kw):
+    g8, gf, gn, o8, of, on = run_both(vol, cam, light, cfg, ctf, otf, w, h, **kw)
+    assert gn == on, (gn, on)
+    assert_rgba8_parity(g8, o8)
+    assert np.array_equal(gf, of, equal_nan=True)
+    return g8, gf
+
+
+@pytest.mark.parametrize("dtype", ["f16", "f32"])
+@pytest.mark.parametrize("normals", [True, False])
+def test_nan_and_inf_voxels(dtype, normals):
+    # NaN and +-inf voxels (and the NaN normals numpy.gradient makes of them):
+    # kernel and oracle take the same path through LUT addressing, skipping
+    # and compositing
+    data = W.value_noise((20, 24, 28), seed=21).astype(np.float32)
+    data[5:8, 6:9, 7:10] = np.nan
+    data[12, 3:20, 4] = np.inf
+    data[15:17, 10:12, 20:22] = -np.inf
+    data = data.astype(np.float16 if dtype == "f16" else np.float32)
+    with np.errstate(invalid="ignore"):
+        nrm = compute_normal_volume(data) if normals else None
+    vol = Volume(data=data, normals=nrm, min_bounds=np.full(3, -1.0, np.float32),
+                 max_bounds=np.full(3, 1.0, np.float32))
+    cam = Camera.from_spherical(np.zeros(3, np.float32), 0.6, 0.3, 0.0, 3.0)
+    for otf in (OpacityTransferFunction.linear(0.0, 0.3), OpacityTransferFunction.peaks([0.4], opacity=0.5)):
+        g8, gf = _check_nan_equal(vol, cam, Light.default(), RenderConfig.balanced(), W.standin_colormap(2),
+                                  otf, 48, 40)
+        assert np.isnan(gf).any() or (g8[..., 3] > 0).any()
+
+
+@pytest.mark.parametrize("w,h", [(1000, 17), (17, 1000), (1, 333), (257, 255)])
+def test_ragged_image_sizes(w, h):
+    c = W.config_small()
+    check(c["volume"], c["camera"], c["light"], c["config"], c["ctf"], c["otf"], w, h)
+
+
+def test_largest_serving_volume_row_band():
+    # 512^3 uint8 (the largest serving volume), 1024^2 high_quality, a band
+    # of rows against the oracle; no normal volume (shading from the density)
+    data = W.to_storage(W.value_noise_device(512, 77), "u8")
+    vol = Volume(data=data, min_bounds=np.full(3, -1.0, np.float32), max_bounds=np.full(3, 1.0, np.float32))
+    cam = Camera.from_spherical(np.zeros(3, np.float32), 1.1, 0.4, 0.0, 3.0)
+    ctf, otf = W.standin_colormap(5), W.random_opacity(np.random.default_rng(9), 8, 0.3)
+    cfg, light = RenderConfig.high_quality(), Light.directional([1, -1, 0], 0.2, 0.8)
+    with VolumeRenderer(1024, 1024, config=cfg, light=light) as r:
+        r.load_volume(vol, value_scale=1 / 255)
+        r.set_camera(cam)
+        r.set_transfer_functions(ctf, otf)
+        g8, gf = r.render_float()
+    s = W.frame_inputs(vol, cam, light, cfg, rgba_lut(ctf, otf), 1024, 1024, 1 / 255)
+    rows = (600, 608)
+    o8, of, _ = oracle.render(s, rows=rows)
+    assert_rgba8_parity(g8[rows[0]:rows[1]], o8[rows[0]:rows[1]])
+    assert np.array_equal(gf[rows[0]:rows[1]], of[rows[0]:rows[1]])
+    assert (g8[rows[0]:rows[1], :, 3] > 0).mean() > 0.2
