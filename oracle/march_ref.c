@@ -27,7 +27,11 @@
  *   - division by the box extent is a multiply by its float reciprocal;
  *   - step/reference_step_size is folded into one float factor;
  *   - exp is oracle_expf below (Cody-Waite reduction + degree-7 Taylor);
- *   - normalize(v) = v * (1/sqrtf(dot(v,v))); a zero vector shades with a
+ *   - normalize(v) = v * rsqrt(dot(v,v)) with the reciprocal square root
+ *     rounded once to float, computed as (float)(1.0 / sqrt((double)x))
+ *     (the double quotient is rounded to the same float as the exact value
+ *     for every positive float input: checked exhaustively against the
+ *     GPU's correctly rounded __frsqrt_rn); a zero vector shades with a
  *     diffuse term of 0 (what max(dot(NaN, L), 0) gives under IEEE maxNum);
  *   - UNORM8 store = rintf(x * 255) of the clamped blended value.
  * Build with -ffp-contract=off.  No image-level golden data exists for this
@@ -263,7 +267,7 @@ static int march_pixel(const OracleScene *s, const Derived *dv, int px, int py, 
             float n2 = (n[0] * n[0] + n[1] * n[1]) + n[2] * n[2];
             float di = 0.0f;                            /* frag:107-110 */
             if (n2 > 0.0f) {
-                float inv = 1.0f / sqrtf(n2);
+                float inv = (float)(1.0 / sqrt((double)n2));
                 float d = ((n[0] * inv) * dv->light_dir[0] + (n[1] * inv) * dv->light_dir[1])
                         + (n[2] * inv) * dv->light_dir[2];
                 di = fmaxf(d, 0.0f);

@@ -177,7 +177,8 @@ def render_view(volume, lut, scene: dict, normals=None, dtype=torch.float32):
                 n = torch.stack([dd, torch.zeros_like(dd), torch.zeros_like(dd)], 1)
             n2 = (n[:, 0] * n[:, 0] + n[:, 1] * n[:, 1]) + n[:, 2] * n[:, 2]
             safe = torch.where(n2 > 0, n2, torch.ones_like(n2))
-            inv = 1.0 / torch.sqrt(safe)
+            # reciprocal square root rounded once (as the kernel's __frsqrt_rn)
+            inv = (1.0 / torch.sqrt(safe.double())).to(dt)
             dd_ = ((n[:, 0] * inv) * light_dir[0] + (n[:, 1] * inv) * light_dir[1]) + (n[:, 2] * inv) * light_dir[2]
             di = torch.where(n2 > 0, torch.clamp(dd_, min=0.0), torch.zeros_like(dd_))
             light = amb + dif * di

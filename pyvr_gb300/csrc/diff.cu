@@ -160,7 +160,7 @@ __device__ __forceinline__ void eval_sample(const DiffParams &p, const MarchFram
     const float n2 = __fadd_rn(__fadd_rn(__fmul_rn(n[0], n[0]), __fmul_rn(n[1], n[1])), __fmul_rn(n[2], n[2]));
     float di = 0.0f;
     if (n2 > 0.0f) {
-        const float inv = __fdiv_rn(1.0f, __fsqrt_rn(n2));
+        const float inv = __frsqrt_rn(n2);  // as the renderer: rsqrt rounded once
         const float d = __fadd_rn(__fadd_rn(__fmul_rn(__fmul_rn(n[0], inv), f.light_dir[0]),
                                             __fmul_rn(__fmul_rn(n[1], inv), f.light_dir[1])),
                                   __fmul_rn(__fmul_rn(n[2], inv), f.light_dir[2]));
