@@ -69,7 +69,7 @@ def parse_args():
     ap.add_argument("--probe-s", type=float, default=2.0, help="seconds per rate probe")
     ap.add_argument("--refine", type=int, default=3, help="bisection probes after the doubling sweep")
     ap.add_argument("--slots", type=int, default=3, help="server: batches in flight")
-    ap.add_argument("--linger-us", type=int, default=200, help="server: hold a partial batch this long")
+    ap.add_argument("--linger-us", type=int, default=100, help="server: hold a partial batch this long")
     ap.add_argument("--serving-volumes", type=int, default=32)
     ap.add_argument("--serving-max-dim", type=int, default=512)
     ap.add_argument("--serving-extra", type=int, default=16, help="volumes outside the catalog (loads)")

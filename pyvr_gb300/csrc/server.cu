@@ -58,7 +58,7 @@ struct Slot {
     cudaEvent_t done = nullptr, k0 = nullptr, k1 = nullptr;
     void *d_arena = nullptr;
     void *h_arena = nullptr;
-    size_t cap = 0;
+    size_t cap = 0, hcap = 0;
     unsigned long long *d_counters = nullptr;
     unsigned long long *h_counters = nullptr;
     std::vector<Req> reqs;
@@ -95,21 +95,31 @@ using pvr::fail;
 
 namespace {
 
+// The slot's device image arena grows in stream order (no host
+// synchronisation: the old arena is freed behind the work already queued).
 int ensure_arena(Slot &s, size_t need) {
     if (need <= s.cap) return PVR_OK;
     size_t cap = 32u << 20;  // 24 images of 512^2 or 8 of 1024^2 before any growth
     while (cap < need) cap <<= 1;
     if (s.d_arena) PVR_CUDA(cudaFreeAsync(s.d_arena, s.stream));
-    if (s.h_arena) {
-        PVR_CUDA(cudaStreamSynchronize(s.stream));
-        cudaFreeHost(s.h_arena);
-    }
     s.d_arena = nullptr;
-    s.h_arena = nullptr;
     s.cap = 0;
     PVR_CUDA(cudaMallocAsync(&s.d_arena, cap, s.stream));
-    PVR_CUDA(cudaHostAlloc(&s.h_arena, cap, cudaHostAllocPortable));
     s.cap = cap;
+    return PVR_OK;
+}
+
+// The pinned staging arena, for destinations that are not page-locked only.
+// The slot is idle when the scheduler fills it, so the old arena is free.
+int ensure_host_arena(Slot &s, size_t need) {
+    if (need <= s.hcap) return PVR_OK;
+    size_t cap = 32u << 20;
+    while (cap < need) cap <<= 1;
+    if (s.h_arena) cudaFreeHost(s.h_arena);
+    s.h_arena = nullptr;
+    s.hcap = 0;
+    PVR_CUDA(cudaHostAlloc(&s.h_arena, cap, cudaHostAllocPortable));
+    s.hcap = cap;
     return PVR_OK;
 }
 
@@ -134,6 +144,12 @@ void fill_from_request(const pvr_request &r, pvr_job &j) {
 // the scheduler's half of one batch: returns the status of the launch
 int launch_slot(pvr_server *srv, Slot &s) {
     const int n = (int)s.reqs.size();
+    // the persistent kernel drains one tile queue in job order: the most
+    // expensive renders (pixels x samples per unit length) go first, so that
+    // no long render starts at the end of the launch
+    std::stable_sort(s.reqs.begin(), s.reqs.end(), [](const Req &a, const Req &b) {
+        return (double)a.r.width * a.r.height / a.r.step_size > (double)b.r.width * b.r.height / b.r.step_size;
+    });
     s.offs.resize(n);
     s.jobs.resize(n);
     size_t total = 0;
@@ -174,7 +190,10 @@ int launch_slot(pvr_server *srv, Slot &s) {
         else
             staged = true;
     }
-    if (staged) PVR_CUDA(cudaMemcpyAsync(s.h_arena, s.d_arena, total, cudaMemcpyDeviceToHost, s.stream));
+    if (staged) {
+        if (int rc = ensure_host_arena(s, total)) return rc;
+        PVR_CUDA(cudaMemcpyAsync(s.h_arena, s.d_arena, total, cudaMemcpyDeviceToHost, s.stream));
+    }
     PVR_CUDA(cudaEventRecord(s.done, s.stream));
     return PVR_OK;
 }

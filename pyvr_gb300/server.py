@@ -30,6 +30,7 @@ from __future__ import annotations
 
 import collections
 import ctypes
+import gc
 import queue
 import threading
 import time
@@ -792,6 +793,18 @@ def drive(impl, stream, timeout: float = 300.0):
     reqs = [RenderRequest(**kw) for _, kw in stream]
     if not reqs:
         return reqs, 0.0
+    # the request objects (and everything else alive now) are moved out of the
+    # cyclic collector's reach for the replay, so that no collection pause
+    # falls between a request's arrival stamp and its submission
+    gc.collect()
+    gc.freeze()
+    try:
+        return _replay(impl, stream, reqs, timeout)
+    finally:
+        gc.unfreeze()
+
+
+def _replay(impl, stream, reqs, timeout):
     if not isinstance(impl, SerialRenderer):
         t0 = time.perf_counter()
         for (off, _), req in zip(stream, reqs):
