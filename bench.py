@@ -234,7 +234,8 @@ def serving_section(args, torch):
         st = latency_stats(reqs)
         st["completed_per_s"] = len(reqs) / el
         nom[name] = st
-    # untimed sweep: highest rate with p99 <= 20 ms
+    # untimed sweep: highest rate with p99 <= 20 ms (a failing probe is
+    # repeated once)
     rates = [NOMINAL_RATE * (2 ** k) for k in range(8)]
     r_server, probes_server = sustained_rate(server, wl, rates, args.probe_s, 300, refine=args.refine)
     r_serial, probes_serial = sustained_rate(serial, wl, rates, args.probe_s, 400, refine=args.refine)

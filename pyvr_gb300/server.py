@@ -847,17 +847,22 @@ def sustained_rate(impl, workload, rates, probe_s: float, seed: int, p99_ms: flo
     """Highest offered rate that `impl` serves with p99 latency <= p99_ms and
     completions keeping up with arrivals: probes `rates` (ascending) up to the
     first failure, then bisects `refine` times between the last passing and
-    the first failing rate.  Returns (rate or None, [probe results])."""
+    the first failing rate.  A failing probe is repeated once (another stream
+    at the same rate), so that one transient stall does not end the sweep.
+    Returns (rate or None, [probe results])."""
     probes = []
 
     def probe(rate, k):
-        stream = workload.requests(rate, probe_s, seed + k)
-        reqs, elapsed = drive(impl, stream)
-        st = latency_stats(reqs)
-        st.update(offered=rate, completed_per_s=len(reqs) / elapsed if elapsed else 0.0)
-        st["ok"] = bool(st.get("p99_ms", 1e9) <= p99_ms and st["completed_per_s"] >= 0.9 * rate)
-        probes.append(st)
-        return st["ok"]
+        for attempt in range(2):
+            stream = workload.requests(rate, probe_s, seed + k + 1000 * attempt)
+            reqs, elapsed = drive(impl, stream)
+            st = latency_stats(reqs)
+            st.update(offered=rate, completed_per_s=len(reqs) / elapsed if elapsed else 0.0, repeat=attempt)
+            st["ok"] = bool(st.get("p99_ms", 1e9) <= p99_ms and st["completed_per_s"] >= 0.9 * rate)
+            probes.append(st)
+            if st["ok"]:
+                return True
+        return False
 
     best, fail = None, None
     for rate in rates:
