@@ -254,12 +254,14 @@ def serving_section(args, torch):
             barrier()
             impl.reset_stats()
             m0 = impl.luts.misses
+            up0 = impl.cache.uploaded_bytes
             reqs, el = drive(impl, wl.requests(rate, float(args.steps), seed))
             torch.cuda.synchronize()
             barrier()
             lat = latency_stats(reqs)
             attempts.append({"offered": rate, "completed_per_s": len(reqs) / el, "p99_ms": lat.get("p99_ms"),
-                             "lut_builds": impl.luts.misses - m0})
+                             "lut_builds": impl.luts.misses - m0,
+                             "uploaded_bytes": impl.cache.uploaded_bytes - up0})
             if lat.get("p99_ms", 1e9) <= P99_MS:
                 break
             rate *= 0.9
@@ -279,9 +281,10 @@ def serving_section(args, torch):
     k_ms = st["kernel_ms"]
     achieved = st["algorithmic_bytes"] / (k_ms / 1000.0) / 1e9 if k_ms else 0.0
     d2h = sum(r.width * r.height * 4 for r in srv_reqs)
-    # uploads: new volumes (tables of new transfer functions are built on the
-    # device from their control points, passed as kernel parameters)
-    h2d = sum(r.volume.data.nbytes for r in srv_reqs if r.tag == "load")
+    # uploads: volumes not yet resident (tables of new transfer functions are
+    # built on the device from their control points, passed as kernel
+    # parameters)
+    h2d = srv_attempts[-1]["uploaded_bytes"]
     out = dict(value=len(srv_reqs) / srv_el, serial_value=len(ser_reqs) / ser_el,
                counts=(len(srv_reqs), srv_el, len(ser_reqs), ser_el),
                lut_builds=srv_attempts[-1]["lut_builds"], launches=launches,

@@ -82,6 +82,7 @@ class VolumeCache:
         self._lock = threading.Lock()
         self.evictions = 0
         self.loads = 0
+        self.uploaded_bytes = 0  # host bytes of the volumes uploaded so far
 
     @property
     def used(self) -> int:
@@ -140,6 +141,7 @@ class VolumeCache:
             self._vols[vid] = dv
             self._bytes[vid] = dv.device_bytes()
             self.loads += 1
+            self.uploaded_bytes += int(volume.data.nbytes)
         return dv
 
 
