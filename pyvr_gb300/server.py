@@ -3,8 +3,9 @@
 The reference renders one frame per call on one GL context
 (pyvr/moderngl_renderer/renderer.py:209-219) from an interactive loop
 (pyvr/interface/matplotlib_interface.py:168-247: orbit re-renders, TF edits,
-high-quality captures).  ``RenderServer`` serves that access pattern for many
-clients at once:
+high-quality captures).  ``RenderServer`` (= ``NativeRenderServer``, on the
+native serving runtime) and ``PyRenderServer`` (the same design with a
+Python scheduler) serve that access pattern for many clients at once:
 
 * volumes stay resident in HBM as march records (``DeviceVolume``); a byte
   budget is enforced with LRU eviction, and an evicted volume's memory is
@@ -260,8 +261,9 @@ class _Pool:
         self._free[key].append(obj)
 
 
-class RenderServer:
-    """Continuous-batching render server (see module docstring)."""
+class PyRenderServer:
+    """Continuous-batching render server with its scheduler in Python (see
+    the module docstring); ``RenderServer`` is the native one."""
 
     def __init__(self, budget_bytes: int = 40 << 30, max_batch: int = 64, slots: int = 3,
                  tuning: Optional[Tuning] = None, brick_log2: int = 3, loaders: int = 2,
@@ -882,3 +884,7 @@ def sustained_rate(impl, workload, rates, probe_s: float, seed: int, p99_ms: flo
                 hi = mid
         best = lo
     return best, probes
+
+
+# the serving API: the native runtime
+RenderServer = NativeRenderServer

@@ -7,7 +7,7 @@ import pytest
 import oracle
 from pyvr_gb300 import workloads as W
 from pyvr_gb300.renderer import rgba_lut
-from pyvr_gb300.server import RenderRequest, RenderServer, SerialRenderer, latency_stats
+from pyvr_gb300.server import PyRenderServer, RenderRequest, SerialRenderer, latency_stats
 
 pytestmark = pytest.mark.gpu
 
@@ -22,7 +22,7 @@ def _workload():
 def _run(budget, n_req=160):
     wl = _workload()
     stream = wl.requests(rate=4000.0, duration=1.0, seed=3)[:n_req]
-    server = RenderServer(budget_bytes=budget, max_batch=16, slots=3)
+    server = PyRenderServer(budget_bytes=budget, max_batch=16, slots=3)
     serial = SerialRenderer()
     for slot in range(wl.n_catalog):
         vol, vs = wl.volumes[slot]
