@@ -56,6 +56,31 @@ def test_null_handle_errors(native_lib):
     assert not out.value
 
 
+def test_argument_checks_before_any_device_work(native_lib):
+    """Entry points added beside the renderer reject bad arguments up front
+    (no device is touched, so these run anywhere)."""
+    lib = native_lib
+    V, E = _native.PVR_OK, _native.PVR_ERR_VALUE
+    out = ctypes.c_void_p()
+    cfg = _native.PvrServerConfig(0, 3, 0, 0, 0, _native.PvrTuning(0, 0, 0, 0))
+    assert lib.pvr_server_create(ctypes.byref(cfg), ctypes.byref(out)) == E and not out.value
+    cfg = _native.PvrServerConfig(8, 99, 0, 0, 0, _native.PvrTuning(0, 0, 0, 0))
+    assert lib.pvr_server_create(ctypes.byref(cfg), ctypes.byref(out)) == E
+    assert lib.pvr_server_create(None, ctypes.byref(out)) == E
+    req = _native.PvrRequest()
+    assert lib.pvr_server_submit(None, ctypes.byref(req)) == E
+    n = ctypes.c_int(0)
+    assert lib.pvr_server_poll(None, None, 1, 0, ctypes.byref(n)) == E
+    assert lib.pvr_server_destroy(None) == V
+    assert lib.pvr_lut_build(None, None, None, 1, None, None, 1, 256, None) == E
+    assert lib.pvr_diff_forward(None, None, None, None) == E
+    scene = _native.PvrDiffScene()
+    assert lib.pvr_diff_forward(ctypes.byref(scene), None, None, None) == E  # no volume / LUT / views
+    assert lib.pvr_batch_render_static(None, 1, None, None) == E
+    assert lib.pvr_batch_render_static(None, -1, None, None) == E
+    assert lib.pvr_batch_render(None, None, 0, None) == E
+
+
 def test_error_code_mapping():
     for code, exc in [(_native.PVR_ERR_VALUE, ValueError), (_native.PVR_ERR_TYPE, TypeError),
                       (_native.PVR_ERR_STATE, RuntimeError), (_native.PVR_ERR_NOMEM, MemoryError),
