@@ -47,7 +47,8 @@ typedef struct pvr_volume pvr_volume;
 typedef struct pvr_lut pvr_lut;
 typedef struct pvr_batch pvr_batch;
 
-/* Library identity. */
+/* Library identity and the calling thread's last error message (no
+ * counterpart in the reference, which raises Python exceptions directly). */
 int pvr_abi_version(void);
 const char *pvr_last_error(void);
 
@@ -165,7 +166,9 @@ int pvr_volume_destroy(pvr_volume *v);   /* waits for the whole device first */
  * invalid on return. */
 int pvr_volume_release(pvr_volume *v, void *stream);
 int pvr_volume_device_bytes(const pvr_volume *v, long long *bytes);
-/* The float32 (D,H,W,3) normals held in the records (host buffer). */
+/* The float32 (D,H,W,3) normals held in the records (host buffer): what
+ * Volume.normals holds after compute_normal_volume (pyvr/volume/data.py:103-118),
+ * read back from the device. */
 int pvr_volume_read_normals(const pvr_volume *v, float *normals_out);
 
 /* The combined RGBA table of create_rgba_transfer_function_texture
@@ -213,7 +216,9 @@ typedef struct pvr_tuning_s {
     int tile_w, tile_h, steps_per_iter, blocks_per_sm;
 } pvr_tuning;
 
-/* A batch launcher with `slots` staging slots (batches that may be in flight
+/* ---- Batches (no counterpart in the reference, which renders one frame per
+ * GL draw: renderer.py:209-219) -----------------------------------------
+ * A batch launcher with `slots` staging slots (batches that may be in flight
  * at once).  Each batch is one persistent kernel over a shared work queue of
  * pixel tiles, launched as a captured CUDA graph. */
 int pvr_batch_create(int capacity_jobs, int slots, pvr_batch **out);
