@@ -214,7 +214,8 @@ def serving_section(args, torch):
     wl = W.ServingWorkload(n_volumes=args.serving_volumes, n_extra=args.serving_extra, min_dim=128,
                            max_dim=args.serving_max_dim, seed=0)
     pin_host_volumes(wl, torch)
-    server = NativeRenderServer(budget_bytes=40 << 30, max_batch=64, slots=args.slots, instrument=True,
+    # kernel events and sample counters on every 8th batch (the roofline)
+    server = NativeRenderServer(budget_bytes=40 << 30, max_batch=64, slots=args.slots, instrument=8,
                                 linger_us=args.linger_us)
     serial = NativeRenderServer(budget_bytes=40 << 30, per_frame=True)
     for slot in range(wl.n_catalog):
@@ -227,9 +228,15 @@ def serving_section(args, torch):
     for w in range(args.warmup):
         drive(server, wl.requests(NOMINAL_RATE, 1.0, 100 + w))
         drive(serial, wl.requests(NOMINAL_RATE, 1.0, 150 + w))
+    # the workload's state (catalog churn, orbits, TF edits) evolves with every
+    # stream: each measurement below restarts from this point, so that all
+    # of them see the same mix
+    snap = wl.snapshot()
+    reset = lambda: wl.restore(snap)  # noqa: E731
     # latency at the nominal rate, both (reported, untimed)
     nom = {}
     for name, impl in (("server", server), ("serial", serial)):
+        reset()
         reqs, el = drive(impl, wl.requests(NOMINAL_RATE, 3.0, 200))
         st = latency_stats(reqs)
         st["completed_per_s"] = len(reqs) / el
@@ -237,8 +244,10 @@ def serving_section(args, torch):
     # untimed sweep: highest rate with p99 <= 20 ms (a failing probe is
     # repeated once)
     rates = [NOMINAL_RATE * (2 ** k) for k in range(8)]
-    r_server, probes_server = sustained_rate(server, wl, rates, args.probe_s, 300, refine=args.refine)
-    r_serial, probes_serial = sustained_rate(serial, wl, rates, args.probe_s, 400, refine=args.refine)
+    r_server, probes_server = sustained_rate(server, wl, rates, args.probe_s, 300, refine=args.refine,
+                                             reset=reset)
+    r_serial, probes_serial = sustained_rate(serial, wl, rates, args.probe_s, 300, refine=args.refine,
+                                             reset=reset)
     r_server = r_server or NOMINAL_RATE
     r_serial = r_serial or NOMINAL_RATE
     # timed: K one-second steps at the sustained rate, server then serial
@@ -255,6 +264,7 @@ def serving_section(args, torch):
             impl.reset_stats()
             m0 = impl.luts.misses
             up0 = impl.cache.uploaded_bytes
+            reset()
             reqs, el = drive(impl, wl.requests(rate, float(args.steps), seed))
             torch.cuda.synchronize()
             barrier()
@@ -268,7 +278,7 @@ def serving_section(args, torch):
         return reqs, el, impl.stats(), attempts
 
     srv_reqs, srv_el, st, srv_attempts = timed_run(server, r_server, 500)
-    ser_reqs, ser_el, _, ser_attempts = timed_run(serial, r_serial, 600)
+    ser_reqs, ser_el, _, ser_attempts = timed_run(serial, r_serial, 500)
     clk = clocks.stop()
     # our kernels in the timed region: batch marches (server), single-render
     # marches (per-frame), LUT builds of new transfer functions (both)
@@ -294,13 +304,15 @@ def serving_section(args, torch):
                batches=st["batches"],
                mean_batch=st["jobs"] / max(1, st["batches"]), max_batch=st["max_jobs"],
                kernel_ms=k_ms, inbox_samples=st["inbox_samples"], shaded_samples=st["shaded_samples"],
-               mean_inbox_per_request=st["inbox_samples"] / max(1, st["jobs"]),
-               gpu_busy_frac=k_ms / 1000.0 / srv_el,
+               mean_inbox_per_request=st["inbox_samples"] / max(1, st["instrumented_jobs"]),
+               gpu_busy_frac=k_ms * st["batches"] / max(1, st["instrumented_batches"]) / 1000.0 / srv_el,
                roofline={"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
-                         "traffic": SERVING_DRAM_BYTES_PER_SAMPLE * st["shaded_samples"] / max(1, st["batches"]),
+                         "traffic": SERVING_DRAM_BYTES_PER_SAMPLE * st["shaded_samples"]
+                         / max(1, st["instrumented_batches"]),
                          "traffic_note": "per launch, scaled from a reduced-catalog ncu capture by samples",
-                         "algorithmic_bytes_per_launch": st["algorithmic_bytes"] / max(1, st["batches"]),
+                         "algorithmic_bytes_per_launch": st["algorithmic_bytes"] / max(1, st["instrumented_batches"]),
+                         "launches_timed": st["instrumented_batches"],
                          "kernel": "march_batch_kernel",
                          "note": "batches in flight on different streams may overlap; summed launch "
                                  "times make this a lower bound"},

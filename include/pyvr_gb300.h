@@ -330,7 +330,7 @@ typedef struct {
     int max_batch;              /* requests per batch (1..4096) */
     int slots;                  /* batches in flight (1..16) */
     int per_frame;              /* 1: per-frame baseline */
-    int instrument;             /* 1: kernel events and sample counters per batch */
+    int instrument;             /* N > 0: kernel events and sample counters on every N-th batch */
     int linger_us;              /* with a batch in flight, hold a partial batch up to this long */
     pvr_tuning tuning;          /* tile_w == 0: default */
 } pvr_server_config;
@@ -338,10 +338,11 @@ typedef struct {
 typedef struct {
     long long submitted, batches, jobs;
     int max_jobs;
-    double kernel_ms;           /* summed batch-kernel event times (instrument) */
-    long long inbox_samples, shaded_samples;
-    double algorithmic_bytes;   /* shaded samples x (8 voxel + 8 x 12 normal bytes) */
+    double kernel_ms;           /* summed batch-kernel event times of the instrumented batches */
+    long long inbox_samples, shaded_samples;   /* ... their in-box / shaded samples */
+    double algorithmic_bytes;   /* ... shaded samples x (8 voxel + 8 x 12 normal bytes) */
     long long queued;
+    long long instrumented_batches, instrumented_jobs;
 } pvr_server_stats;
 
 int pvr_server_create(const pvr_server_config *cfg, pvr_server **out);

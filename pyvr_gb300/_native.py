@@ -183,7 +183,8 @@ class PvrServerConfig(ctypes.Structure):
 class PvrServerStats(ctypes.Structure):
     """pvr_server_stats of include/pyvr_gb300.h."""
     _fields_ = [("submitted", _LL), ("batches", _LL), ("jobs", _LL), ("max_jobs", _I), ("kernel_ms", _D),
-                ("inbox_samples", _LL), ("shaded_samples", _LL), ("algorithmic_bytes", _D), ("queued", _LL)]
+                ("inbox_samples", _LL), ("shaded_samples", _LL), ("algorithmic_bytes", _D), ("queued", _LL),
+                ("instrumented_batches", _LL), ("instrumented_jobs", _LL)]
 
 
 class PvrDiffView(ctypes.Structure):

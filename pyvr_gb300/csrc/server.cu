@@ -65,6 +65,7 @@ struct Slot {
     std::vector<size_t> offs;
     std::vector<pvr_job> jobs;
     int status = PVR_OK;
+    bool instrumented = false;  // this batch records kernel events and counters
 };
 
 int bytes_per_sample(int dtype) {
@@ -89,6 +90,7 @@ struct pvr_server {
     std::thread sched, completer;
     pvr_server_stats stats;
     std::string last_error;
+    long long batch_seq = 0;  // batches launched (scheduler thread only)
 };
 
 using pvr::fail;
@@ -158,6 +160,8 @@ int launch_slot(pvr_server *srv, Slot &s) {
         total += ((size_t)s.reqs[i].r.width * s.reqs[i].r.height * 4 + 255) & ~(size_t)255;
     }
     if (int rc = ensure_arena(s, total)) return rc;
+    s.instrumented = srv->cfg.instrument > 0 && srv->batch_seq % srv->cfg.instrument == 0;
+    ++srv->batch_seq;
     for (int i = 0; i < n; ++i) {
         void *ev = s.reqs[i].r.wait_event;
         bool seen = false;  // one wait per distinct event
@@ -167,14 +171,14 @@ int launch_slot(pvr_server *srv, Slot &s) {
     for (int i = 0; i < n; ++i) {
         fill_from_request(s.reqs[i].r, s.jobs[i]);
         s.jobs[i].d_rgba8 = (char *)s.d_arena + s.offs[i];
-        s.jobs[i].d_counters = srv->cfg.instrument ? s.d_counters + 2 * i : nullptr;
+        s.jobs[i].d_counters = s.instrumented ? s.d_counters + 2 * i : nullptr;
     }
-    if (srv->cfg.instrument) {
+    if (s.instrumented) {
         PVR_CUDA(cudaMemsetAsync(s.d_counters, 0, sizeof(unsigned long long) * 2 * n, s.stream));
         PVR_CUDA(cudaEventRecord(s.k0, s.stream));
     }
     if (int rc = pvr_batch_render(s.batch, s.jobs.data(), n, s.stream)) return rc;
-    if (srv->cfg.instrument) {
+    if (s.instrumented) {
         PVR_CUDA(cudaEventRecord(s.k1, s.stream));
         PVR_CUDA(cudaMemcpyAsync(s.h_counters, s.d_counters, sizeof(unsigned long long) * 2 * n,
                                  cudaMemcpyDeviceToHost, s.stream));
@@ -276,13 +280,13 @@ void completer_loop(pvr_server *srv) {
             out[i].t_submit_ns = s.reqs[i].t_submit;
             out[i].t_launch_ns = s.reqs[i].t_launch;
             out[i].t_done_ns = t_done;
-            if (status == PVR_OK && srv->cfg.instrument) {
+            if (status == PVR_OK && s.instrumented) {
                 inbox += (long long)s.h_counters[2 * i];
                 shaded += (long long)s.h_counters[2 * i + 1];
                 alg += (double)s.h_counters[2 * i + 1] * bytes_per_sample(r.volume->dtype);
             }
         }
-        if (status == PVR_OK && srv->cfg.instrument) cudaEventElapsedTime(&kms, s.k0, s.k1);
+        if (status == PVR_OK && s.instrumented) cudaEventElapsedTime(&kms, s.k0, s.k1);
         lk.lock();
         srv->stats.batches += 1;
         srv->stats.jobs += (long long)s.reqs.size();
@@ -291,6 +295,10 @@ void completer_loop(pvr_server *srv) {
         srv->stats.inbox_samples += inbox;
         srv->stats.shaded_samples += shaded;
         srv->stats.algorithmic_bytes += alg;
+        if (s.instrumented) {
+            srv->stats.instrumented_batches += 1;
+            srv->stats.instrumented_jobs += (long long)s.reqs.size();
+        }
         for (auto &c : out) srv->completions.push_back(c);
         s.reqs.clear();
         srv->inflight.pop_front();

@@ -575,11 +575,12 @@ class NativeRenderServer:
     A result is the request's RGBA8 image as a flat uint8 array (H*W*4,
     bottom row first: the bytes ``render()`` returns).  per_frame=True is
     the per-frame baseline on the same runtime (one request per launch, each
-    read back before the next starts)."""
+    read back before the next starts).  instrument=N times every N-th batch
+    kernel and counts its samples (``stats()``)."""
 
     def __init__(self, budget_bytes: int = 40 << 30, max_batch: int = 64, slots: int = 3,
                  tuning: Optional[Tuning] = None, brick_log2: int = 3, loaders: int = 2,
-                 instrument: bool = False, per_frame: bool = False, linger_us: int = 0):
+                 instrument: int = 0, per_frame: bool = False, linger_us: int = 0):
         import torch
         self.torch = torch
         self.cache = VolumeCache(budget_bytes, brick_log2)
@@ -847,17 +848,21 @@ def _replay(impl, stream, reqs, timeout):
 
 
 def sustained_rate(impl, workload, rates, probe_s: float, seed: int, p99_ms: float = 20.0,
-                   refine: int = 0):
+                   refine: int = 0, reset=None):
     """Highest offered rate that `impl` serves with p99 latency <= p99_ms and
     completions keeping up with arrivals: probes `rates` (ascending) up to the
     first failure, then bisects `refine` times between the last passing and
     the first failing rate.  A failing probe is repeated once (another stream
     at the same rate), so that one transient stall does not end the sweep.
-    Returns (rate or None, [probe results])."""
+    reset(): called before every probe (e.g. to restart a workload whose
+    state evolves from the same point).  Returns (rate or None, [probe
+    results])."""
     probes = []
 
     def probe(rate, k):
         for attempt in range(2):
+            if reset is not None:
+                reset()
             stream = workload.requests(rate, probe_s, seed + k + 1000 * attempt)
             reqs, elapsed = drive(impl, stream)
             st = latency_stats(reqs)

@@ -242,6 +242,16 @@ class ServingWorkload:
                 "ctf": standin_colormap(int(srng.integers(0, N_STANDIN_COLORMAPS)))})
         self._next_extra = n_volumes
 
+    def snapshot(self):
+        """The evolving state (catalog, session cameras and opacity points), to
+        restart request streams from the same point with ``restore``."""
+        return (list(self.catalog), [dict(s, otf=list(s["otf"])) for s in self.sessions])
+
+    def restore(self, snap) -> None:
+        catalog, sessions = snap
+        self.catalog = list(catalog)
+        self.sessions = [dict(s, otf=list(s["otf"])) for s in sessions]
+
     def camera(self, vidx: int) -> Camera:
         s = self.sessions[vidx]
         return Camera.from_spherical(target=np.zeros(3, np.float32), azimuth=s["az"],

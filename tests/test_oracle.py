@@ -154,3 +154,16 @@ def test_row_subset_matches_full_render():
     part, _, _ = oracle.render(s, rows=(20, 30), want_float=False)
     np.testing.assert_array_equal(full[20:30], part[20:30])
     assert not part[:20].any()
+
+
+def test_serving_workload_snapshot_restarts_the_same_stream():
+    wl = W.ServingWorkload(n_volumes=4, n_extra=2, min_dim=16, max_dim=24,
+                           generator=lambda n, s: W.value_noise((n, n, n), s))
+    snap = wl.snapshot()
+    first = [(kw["volume_id"], kw["tag"], kw["camera"].azimuth, tuple(kw["opacity_tf"].control_points))
+             for _, kw in wl.requests(2000.0, 0.3, 9)]
+    wl.requests(2000.0, 0.3, 10)  # the state moves on
+    wl.restore(snap)
+    again = [(kw["volume_id"], kw["tag"], kw["camera"].azimuth, tuple(kw["opacity_tf"].control_points))
+             for _, kw in wl.requests(2000.0, 0.3, 9)]
+    assert first == again and any(t == "load" for _, t, _, _ in first)

@@ -77,7 +77,7 @@ def _run_native(budget, n_req=160, per_frame=False, max_batch=16):
     wl = _workload()
     stream = wl.requests(rate=4000.0, duration=1.0, seed=3)[:n_req]
     server = NativeRenderServer(budget_bytes=budget, max_batch=max_batch, slots=3, per_frame=per_frame,
-                                instrument=True)
+                                instrument=1)
     serial = SerialRenderer()
     for slot in range(wl.n_catalog):
         vol, vs = wl.volumes[slot]
