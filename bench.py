@@ -69,7 +69,8 @@ def parse_args():
     ap.add_argument("--probe-s", type=float, default=2.0, help="seconds per rate probe")
     ap.add_argument("--refine", type=int, default=3, help="bisection probes after the doubling sweep")
     ap.add_argument("--slots", type=int, default=3, help="server: batches in flight")
-    ap.add_argument("--linger-us", type=int, default=100, help="server: hold a partial batch this long")
+    ap.add_argument("--linger-us", type=int, default=1000, help="server: hold a partial batch this long")
+    ap.add_argument("--serving-brick-log2", type=int, default=4, help="brick size of the resident volumes")
     ap.add_argument("--serving-volumes", type=int, default=32)
     ap.add_argument("--serving-max-dim", type=int, default=512)
     ap.add_argument("--serving-extra", type=int, default=16, help="volumes outside the catalog (loads)")
@@ -216,8 +217,8 @@ def serving_section(args, torch):
     pin_host_volumes(wl, torch)
     # kernel events and sample counters on every 8th batch (the roofline)
     server = NativeRenderServer(budget_bytes=40 << 30, max_batch=64, slots=args.slots, instrument=8,
-                                linger_us=args.linger_us)
-    serial = NativeRenderServer(budget_bytes=40 << 30, per_frame=True)
+                                linger_us=args.linger_us, brick_log2=args.serving_brick_log2)
+    serial = NativeRenderServer(budget_bytes=40 << 30, per_frame=True, brick_log2=args.serving_brick_log2)
     for slot in range(wl.n_catalog):
         vol, vs = wl.volumes[slot]
         server.cache.insert(slot, vol, vs, server._free_volume)
