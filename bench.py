@@ -79,6 +79,10 @@ def parse_args():
     ap.add_argument("--diff-steps", type=int, default=200, help="Adam steps of the differentiation section")
     ap.add_argument("--no-tune", action="store_true", help="batching section: default tuning, no search")
     ap.add_argument("--storages", default=",".join(DTYPES))
+    ap.add_argument("--plain-volume", type=int, default=N_VOL, help="plain section: volume extent")
+    ap.add_argument("--plain-res", type=int, default=RES, help="plain section: image size")
+    ap.add_argument("--plain-config", default="high_quality", choices=["high_quality", "balanced"],
+                    help="plain section: RenderConfig preset")
     ap.add_argument("--cameras", type=int, default=16)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
@@ -478,19 +482,22 @@ def diff_section(args, torch):
 # Plain per-frame renderer (nested section)
 # ---------------------------------------------------------------------------
 
-def make_scenes(storages=DTYPES):
+def make_scenes(storages=DTYPES, n=N_VOL, res=RES):
     from pyvr_gb300 import workloads as W
-    noise = W.config_scale_volume(N_VOL)
-    return {dt: W.config_scale(dt, n=N_VOL, res=RES, noise=noise) for dt in storages}
+    noise = W.config_scale_volume(n)
+    return {dt: W.config_scale(dt, n=n, res=res, noise=noise) for dt in storages}
 
 
 def plain_section(args, torch):
     from pyvr_gb300 import VolumeRenderer, _native
-    scenes = make_scenes(tuple(args.storages.split(",")))
+    n_vol, res = args.plain_volume, args.plain_res
+    scenes = make_scenes(tuple(args.storages.split(",")), n_vol, res)
     lib = _native.load()
     rend = {}
+    from pyvr_gb300 import RenderConfig
     for dt, c in scenes.items():
-        r = VolumeRenderer(RES, RES, config=c["config"], light=c["light"])
+        c["config"] = getattr(RenderConfig, args.plain_config)()
+        r = VolumeRenderer(res, res, config=c["config"], light=c["light"])
         r.load_volume(c["volume"], value_scale=c["value_scale"])
         r.set_transfer_functions(c["ctf"], c["otf"])
         rend[dt] = r
@@ -499,7 +506,7 @@ def plain_section(args, torch):
     # "the renderer's own stream" to the C ABI
     stream = torch.cuda.Stream()
     sptr = ctypes.c_void_p(stream.cuda_stream)
-    out = torch.empty(RES * RES * 4, dtype=torch.uint8, device="cuda")
+    out = torch.empty(res * res * 4, dtype=torch.uint8, device="cuda")
     samples, shaded = {}, {}
     for dt, r in rend.items():
         for k, cam in enumerate(cams):
@@ -564,12 +571,14 @@ def plain_section(args, torch):
             "samples_per_s": sum(samples[(dt, k)] for dt, k, _ in launch_ms) / elapsed,
             "roofline": {"bound": "hbm", "achieved": tot_bytes / tot_s / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": tot_bytes / tot_s / 1e9 / peak, "peak_kind": peak_kind,
-                         "traffic": PLAIN_F32_DRAM_BYTES_PER_FRAME if "f32" in rend else None,
+                         "traffic": (PLAIN_F32_DRAM_BYTES_PER_FRAME
+                                     if "f32" in rend and (n_vol, res, args.plain_config) == (N_VOL, RES, "high_quality")
+                                     else None),
                          "traffic_note": "f32 frame, one full-size ncu launch",
                          "kernel": "march_single_kernel", "per_storage": per_dtype},
             "gpu_launches": len(launch_ms),
-            "config": {"volume": f"{N_VOL}^3 value noise seed 0", "storages": list(rend),
-                       "cameras": len(cams), "resolution": f"{RES}x{RES}", "render_config": "high_quality",
+            "config": {"volume": f"{n_vol}^3 value noise seed 0", "storages": list(rend),
+                       "cameras": len(cams), "resolution": f"{res}x{res}", "render_config": args.plain_config,
                        "frames_per_step": len(rend) * len(cams),
                        "l2": "inputs larger than L2 (208-256 MiB per storage)"}}
 
