@@ -10,8 +10,8 @@ tensors (plumbing only: the kernels are the library's).
 from __future__ import annotations
 
 import ctypes
-from dataclasses import dataclass, field
-from typing import List, Optional, Sequence
+from dataclasses import dataclass
+from typing import Optional, Sequence
 
 import numpy as np
 

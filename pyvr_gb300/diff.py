@@ -19,7 +19,7 @@ given normal volume, or none) are constants of the scene.
 from __future__ import annotations
 
 import ctypes
-from typing import Optional, Sequence
+from typing import Sequence
 
 import numpy as np
 
@@ -86,8 +86,12 @@ def _check_inputs(volume, lut, normals):
         raise TypeError("volume must be a CUDA float32 tensor of shape (D, H, W)")
     if lut.dtype != torch.float32 or lut.dim() != 2 or lut.shape[1] != 4 or not lut.is_cuda:
         raise TypeError("lut must be a CUDA float32 tensor of shape (size, 4)")
-    if normals is not None and (normals.dtype != torch.float32 or tuple(normals.shape) != tuple(volume.shape) + (3,)):
-        raise TypeError("normals must be a float32 tensor of shape (D, H, W, 3)")
+    if normals is not None and (normals.dtype != torch.float32 or not normals.is_cuda or
+                                tuple(normals.shape) != tuple(volume.shape) + (3,)):
+        raise TypeError("normals must be a CUDA float32 tensor of shape (D, H, W, 3)")
+    devices = {volume.device, lut.device} | ({normals.device} if normals is not None else set())
+    if len(devices) != 1:
+        raise ValueError("volume, lut and normals must be on one device")
 
 
 def _march_function():

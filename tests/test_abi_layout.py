@@ -3,7 +3,6 @@ include/pyvr_gb300.h (sizes and every field offset), checked against a
 program compiled from the header with gcc."""
 
 import ctypes
-import os
 import shutil
 import subprocess
 

@@ -75,3 +75,10 @@ def test_autograd_matches_central_differences(normals):
         with torch.no_grad():
             fd = (loss(plus_v, plus_l) - loss(minus_v, minus_l)).item() / (2 * h)
         assert abs(fd - g) <= 1e-5 * max(abs(fd), 1e-3), (which, idx, fd, g)
+
+
+def test_render_views_checks_its_inputs():
+    from pyvr_gb300.diff import _check_inputs
+    vol, lut = torch.zeros((4, 4, 4)), torch.zeros((16, 4))
+    with pytest.raises(TypeError, match="CUDA"):
+        _check_inputs(vol, lut, None)  # host tensors never reach the kernel

@@ -9,7 +9,7 @@ import pytest
 
 import oracle
 from oracle import march_fp64
-from pyvr_gb300 import Camera, Light, RenderConfig, Volume
+from pyvr_gb300 import Camera, Light, RenderConfig
 from pyvr_gb300 import workloads as W
 from pyvr_gb300.renderer import camera_uniforms, rgba_lut
 

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import oracle
-from pyvr_gb300 import (Camera, ColorTransferFunction, Light, OpacityTransferFunction,
+from pyvr_gb300 import (Camera, Light, OpacityTransferFunction,
                         RenderConfig, Volume, VolumeRenderer, compute_normal_volume)
 from pyvr_gb300 import workloads as W
 from pyvr_gb300.renderer import rgba_lut
