@@ -162,11 +162,19 @@ class RenderJob:
     counters: object = None  # torch int64 (2,) zeroed: [in-box, shaded] samples
 
 
-def _ptr(x) -> Optional[int]:
+def _ptr(x, n: int = 0, dtype: str = "", what: str = "buffer") -> Optional[int]:
+    """Device address of an output: None, a raw device pointer (int, taken
+    as it is), or a CUDA tensor of at least n elements of dtype."""
     if x is None:
         return None
     if isinstance(x, int):
         return x
+    if not getattr(x, "is_cuda", False):
+        raise TypeError(f"{what} must be a CUDA tensor or a device pointer")
+    if dtype and str(x.dtype) != f"torch.{dtype}":
+        raise TypeError(f"{what} must be {dtype}, got {x.dtype}")
+    if x.numel() < n or not x.is_contiguous():
+        raise ValueError(f"{what} must be contiguous with at least {n} elements")
     return int(x.data_ptr())
 
 
@@ -242,9 +250,10 @@ def make_job_struct(job: RenderJob, out: Optional[_native.PvrJob] = None) -> _na
     (native double-precision setup), so an oracle scene for a batch render is
     built from ``job_camera_uniforms``."""
     j = out if out is not None else _native.PvrJob()
+    n = int(job.width) * int(job.height) * 4
     fill_job(j, job.volume.handle.value, job.lut.handle.value, job.camera, job.light, job.config,
-             int(job.width), int(job.height), _ptr(job.out_rgba8), _ptr(job.out_rgba32f),
-             _ptr(job.counters))
+             int(job.width), int(job.height), _ptr(job.out_rgba8, n, "uint8", "out_rgba8"),
+             _ptr(job.out_rgba32f, n, "float32", "out_rgba32f"), _ptr(job.counters, 2, "int64", "counters"))
     return j
 
 

@@ -129,3 +129,11 @@ def test_frame_constants_match_oracle_bit_for_bit(native_lib):
         want = oracle.frame_constants(scene)
         # equal values (a structurally zero inverse entry may be +0 or -0)
         np.testing.assert_array_equal(got, want)
+
+
+def test_job_outputs_must_be_device_buffers():
+    torch = pytest.importorskip("torch")
+    from pyvr_gb300.batch import _ptr
+    assert _ptr(None) is None and _ptr(123456) == 123456  # raw device pointers pass as they are
+    with pytest.raises(TypeError, match="CUDA"):
+        _ptr(torch.zeros(64, dtype=torch.uint8), 64, "uint8", "out_rgba8")
