@@ -665,7 +665,7 @@ def run_reference(args):
     if rank != 0:
         return
     from pyvr_gb300 import workloads as W
-    wl = W.ServingWorkload(n_volumes=args.serving_volumes, n_extra=16, min_dim=128,
+    wl = W.ServingWorkload(n_volumes=args.serving_volumes, n_extra=args.serving_extra, min_dim=128,
                            max_dim=args.serving_max_dim, seed=0,
                            generator=lambda n, s: W.value_noise((n, n, n), s))
     times, reqs, samples = [], 0, 0
