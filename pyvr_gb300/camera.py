@@ -207,6 +207,10 @@ class Camera:
         """lookAt with the basis in the first three COLUMNS of a row-major array
         (pyvr/camera/camera.py:292-334); GL reads its bytes column-major."""
         position, up = self.get_camera_vectors()
+        return self._view_from(position, up)
+
+    def _view_from(self, position: np.ndarray, up: np.ndarray) -> np.ndarray:
+        """get_view_matrix from already computed camera vectors."""
         fwd = self.target - position
         fwd = fwd / np.linalg.norm(fwd)
         right = np.cross(fwd, up)

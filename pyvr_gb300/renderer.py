@@ -17,6 +17,7 @@ import numpy as np
 
 from . import _native
 from ._native import check
+from .camera import Camera
 from .config import RenderConfig
 from .lighting import Light
 
@@ -55,10 +56,16 @@ def rgba_lut(color_tf, opacity_tf, size: Optional[int] = None) -> np.ndarray:
 
 
 def camera_uniforms(camera, width: int, height: int):
-    """(view, proj, position) float32 arrays as renderer.py:160-172 sends them."""
-    view = np.ascontiguousarray(camera.get_view_matrix(), dtype=np.float32)
+    """(view, proj, position) float32 arrays as renderer.py:160-172 sends them
+    (this package's Camera computes its camera vectors once for both)."""
+    if isinstance(camera, Camera):
+        pos, up = camera.get_camera_vectors()
+        view = camera._view_from(pos, up)
+    else:
+        view = camera.get_view_matrix()
+        pos, _ = camera.get_camera_vectors()
+    view = np.ascontiguousarray(view, dtype=np.float32)
     proj = np.ascontiguousarray(camera.get_projection_matrix(width / height), dtype=np.float32)
-    pos, _ = camera.get_camera_vectors()
     return view, proj, np.asarray(pos, dtype=np.float32)
 
 
@@ -146,7 +153,6 @@ class CudaVolumeRenderer:
             check(self._lib.pvr_load_normals(self._handle(), nrm.ctypes.data))
 
     def set_camera(self, camera) -> None:
-        from .camera import Camera
         if not _is_kind(camera, Camera, "Camera"):
             raise TypeError(f"Expected Camera instance, got {type(camera)}")
         self.camera = camera
