@@ -75,7 +75,9 @@ def parse_args():
     ap.add_argument("--serving-max-dim", type=int, default=512)
     ap.add_argument("--serving-extra", type=int, default=16, help="volumes outside the catalog (loads)")
     # smaller cases for profiling captures
-    ap.add_argument("--only", choices=["all", "plain", "serving", "diff", "batching"], default="all")
+    ap.add_argument("--only", choices=["all", "plain", "serving", "diff", "batching", "loaders"],
+                    default="all")
+    ap.add_argument("--loaders-volume", type=int, default=256, help="loaders section: volume extent")
     ap.add_argument("--diff-steps", type=int, default=200, help="Adam steps of the differentiation section")
     ap.add_argument("--no-tune", action="store_true", help="batching section: default tuning, no search")
     ap.add_argument("--storages", default=",".join(DTYPES))
@@ -488,6 +490,116 @@ def make_scenes(storages=DTYPES, n=N_VOL, res=RES):
     return {dt: W.config_scale(dt, n=n, res=res, noise=noise) for dt in storages}
 
 
+def loaders_section(args, torch):
+    """The paths either side of the march, each against the host path the
+    reference takes: volume layout with device normals against numpy normals
+    plus their upload, LUT builds on the device against numpy tables plus
+    upload, the FP64 orbit-camera setup against numpy, and .vti reading."""
+    import numpy as np
+    from pyvr_gb300 import Volume, compute_normal_volume
+    from pyvr_gb300.batch import DeviceLUT, DeviceVolume
+    from pyvr_gb300 import workloads as W
+    from pyvr_gb300.batch import fill_camera
+    from pyvr_gb300.renderer import camera_uniforms, rgba_lut
+    from pyvr_gb300.vti import load_vtk_volume, write_vti
+    from pyvr_gb300.camera import Camera
+    out = {}
+
+    def wall(fn, reps=1):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(reps):
+            r = fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t) / reps, r
+
+    # (1) volume layout with normals computed on the device
+    n = args.loaders_volume
+    base = W.value_noise_device(n, 0)
+    loads = {}
+    for dt in ("u8", "f16"):
+        data = W.to_storage(base, dt)
+        vol = Volume(data=data)
+        DeviceVolume(vol, normals="device", brick_log2=4).close()  # warm-up
+        ts = []
+        for _ in range(args.steps):
+            t, dv = wall(lambda: DeviceVolume(vol, normals="device", brick_log2=4))
+            rec_bytes = dv.device_bytes()
+            dv.close()
+            ts.append(t)
+        entry = {"device_ms": 1000 * statistics.median(ts), "voxels": int(data.size),
+                 "device_bytes": rec_bytes, "gvoxels_per_s": data.size / statistics.median(ts) / 1e9}
+        if not args.skip_cpu:
+            t_np, nrm = wall(lambda: compute_normal_volume(data))
+            t_up, dv = wall(lambda: DeviceVolume(Volume(data=data, normals=nrm), normals="given",
+                                                  brick_log2=4))
+            dv.close()
+            entry.update({"host_normals_ms": 1000 * t_np, "host_normals_upload_ms": 1000 * t_up,
+                          "speedup": (t_np + t_up) / statistics.median(ts)})
+        loads[dt] = entry
+    out["volume_load"] = {"volume": f"{n}^3 value noise seed 0, 16^3 bricks", "per_storage": loads,
+                          "note": "wall time of DeviceVolume(...) to a ready layout, pageable upload "
+                                  "included; host path = numpy normals (reference semantics) + upload"}
+
+    # (2) LUTs built on the device from control points
+    rng = np.random.default_rng(1)
+    tfs = [(W.standin_colormap(i % 12), W.random_opacity(rng, int(rng.integers(4, 13)), 0.3))
+           for i in range(200)]
+    stream = torch.cuda.Stream()
+    lut = DeviceLUT.on_device(*tfs[0], 256)
+    for ctf, otf in tfs[:10]:
+        lut.build(ctf, otf, 256, stream)
+    stream.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t = time.perf_counter()
+    e0.record(stream)
+    for ctf, otf in tfs:
+        lut.build(ctf, otf, 256, stream)
+    e1.record(stream)
+    stream.synchronize()
+    t_dev = (time.perf_counter() - t) / len(tfs)
+    t_host, _ = wall(lambda: [lut.update(rgba_lut(c, o, 256)) for c, o in tfs])
+    lut.close()
+    out["lut_build"] = {"entries": 256, "tables": len(tfs), "device_us_per_table": 1e6 * t_dev,
+                        "device_stream_us_per_table": 1000 * e0.elapsed_time(e1) / len(tfs),
+                        "host_us_per_table": 1e6 * t_host / len(tfs),
+                        "note": "device: pvr_lut_build queued per table (host call included); "
+                                "host: numpy to_lut (reference) + pvr_lut_update upload"}
+
+    # (3) orbit camera setup in FP64 (native) against numpy
+    cams = [Camera.from_spherical(np.zeros(3, np.float32), float(a), float(e), 0.0, float(d))
+            for a, e, d in zip(rng.uniform(-np.pi, np.pi, 2000), rng.uniform(-1.4, 1.4, 2000),
+                               rng.uniform(2.5, 4.0, 2000))]
+    view, proj, pos = (ctypes.c_float * 16)(), (ctypes.c_float * 16)(), (ctypes.c_float * 3)()
+    t = time.perf_counter()
+    for c in cams:
+        fill_camera(c, 512, 512, view, proj, pos)
+    t_nat = (time.perf_counter() - t) / len(cams)
+    t = time.perf_counter()
+    for c in cams:
+        camera_uniforms(c, 512, 512)
+    t_np = (time.perf_counter() - t) / len(cams)
+    out["camera_setup"] = {"cameras": len(cams), "native_us": 1e6 * t_nat, "numpy_us": 1e6 * t_np}
+
+    # (4) .vti reading: the reference's loader (host normals) against reading
+    # plus device normals
+    vn = min(n, 256)
+    raw = W.value_noise_device(vn, 2)
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "noise.vti")
+        write_vti(path, raw.astype(np.float32), spacing=(1.0, 1.0, 1.0), compress=True)
+        size = os.path.getsize(path)
+        t_ref, _ = wall(lambda: load_vtk_volume(path))
+        t_read, vol = wall(lambda: load_vtk_volume(path, compute_normals=False))
+        t_dev, dv = wall(lambda: DeviceVolume(vol, normals="device", brick_log2=4))
+        dv.close()
+    out["vti_load"] = {"volume": f"{vn}^3 float32, zlib blocks", "file_bytes": size,
+                       "reference_loader_ms": 1000 * t_ref, "read_ms": 1000 * t_read,
+                       "device_layout_ms": 1000 * t_dev,
+                       "speedup": t_ref / (t_read + t_dev)}
+    return out
+
+
 def plain_section(args, torch):
     from pyvr_gb300 import VolumeRenderer, _native
     n_vol, res = args.plain_volume, args.plain_res
@@ -607,9 +719,11 @@ def run_ours(args):
     plain = plain_section(args, torch) if args.only in ("all", "plain") else None
     diff = diff_section(args, torch) if args.only in ("all", "diff") else None
     batching = batching_section(args, torch) if args.only in ("all", "batching") else None
-    if args.only in ("plain", "diff", "batching"):
+    loaders = loaders_section(args, torch) if args.only in ("all", "loaders") else None
+    if args.only in ("plain", "diff", "batching", "loaders"):
         if rank == 0:
-            print(json.dumps({"plain": plain, "differentiation": diff, "batching_c3": batching}))
+            print(json.dumps({"plain": plain, "differentiation": diff, "batching_c3": batching,
+                              "loaders": loaders}))
         return
     s = serving_section(args, torch)
     value, serial_value = s["value"], s["serial_value"]
@@ -653,7 +767,7 @@ def run_ours(args):
                 "e2e": {"value": value, "unit": "renders/s", "h2d_bytes_per_step": s["h2d"],
                         "d2h_bytes_per_step": s["d2h"]},
                 "gpu_launches": s["launches"],
-                "plain": plain, "batching_c3": batching, "differentiation": diff}
+                "plain": plain, "batching_c3": batching, "differentiation": diff, "loaders": loaders}
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -111,6 +111,14 @@ int pvr_set_config(pvr_renderer *r, float step_size, int max_steps, float refere
  * Synchronous.  With no volume loaded the image is transparent black. */
 int pvr_render(pvr_renderer *r, uint8_t *out_rgba8, float *out_rgba32f);
 
+/* render() (renderer.py:209-219) into the handle's own page-locked RGBA8
+ * image (width*height*4 bytes, allocated on first use): the image comes
+ * back by DMA with no staging copy, and *rgba8 receives its address.  The
+ * buffer stays valid, unchanged, until the next render call on the handle or
+ * pvr_destroy; a binding copies it into the `bytes` it returns.  Synchronous;
+ * the same image as pvr_render. */
+int pvr_render_pinned(pvr_renderer *r, const uint8_t **rgba8);
+
 /* Same march into caller-owned DEVICE buffers on `stream` (NULL = the
  * handle's stream); asynchronous, no host copy.  Either output may be NULL. */
 int pvr_render_device(pvr_renderer *r, void *d_rgba8, void *d_rgba32f, void *stream);

@@ -105,6 +105,7 @@ SIGNATURES = {
     "pvr_set_light": (_I, [_VP, _FP, _FP, _F, _F]),
     "pvr_set_config": (_I, [_VP, _F, _I, _F]),
     "pvr_render": (_I, [_VP, _VP, _VP]),
+    "pvr_render_pinned": (_I, [_VP, ctypes.POINTER(_VP)]),
     "pvr_render_device": (_I, [_VP, _VP, _VP, _VP]),
     "pvr_last_sample_count": (_I, [_VP, ctypes.POINTER(_LL)]),
     "pvr_last_sample_counts": (_I, [_VP, ctypes.POINTER(_LL), ctypes.POINTER(_LL)]),

@@ -27,6 +27,7 @@ struct pvr_renderer {
     // render targets
     uint32_t *d_out8 = nullptr;
     float4 *d_outf = nullptr;
+    uint8_t *h_out8 = nullptr;  // page-locked image of pvr_render_pinned
     unsigned long long *d_counters = nullptr;  // [in-box samples, shaded samples]
 };
 
@@ -150,6 +151,7 @@ int pvr_destroy(pvr_renderer *r) {
     cudaFree(r->d_out8);
     cudaFree(r->d_outf);
     cudaFree(r->d_counters);
+    cudaFreeHost(r->h_out8);
     if (r->stream) cudaStreamDestroy(r->stream);
     delete r;
     return PVR_OK;
@@ -297,6 +299,18 @@ int pvr_render(pvr_renderer *r, uint8_t *out_rgba8, float *out_rgba32f) {
     if (out_rgba32f)
         PVR_CUDA(cudaMemcpyAsync(out_rgba32f, r->d_outf, npx * 16, cudaMemcpyDeviceToHost, r->stream));
     PVR_CUDA(cudaStreamSynchronize(r->stream));
+    return PVR_OK;
+}
+
+int pvr_render_pinned(pvr_renderer *r, const uint8_t **rgba8) {
+    if (int rc = check_handle(r)) return rc;
+    if (!rgba8) return fail(PVR_ERR_VALUE, "rgba8 is NULL");
+    *rgba8 = nullptr;
+    DeviceScope ds(r->device);
+    const size_t npx = (size_t)r->width * r->height;
+    if (!r->h_out8) PVR_CUDA(cudaMallocHost((void **)&r->h_out8, npx * 4));
+    if (int rc = pvr_render(r, r->h_out8, nullptr)) return rc;
+    *rgba8 = r->h_out8;
     return PVR_OK;
 }
 

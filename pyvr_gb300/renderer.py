@@ -197,8 +197,11 @@ class CudaVolumeRenderer:
         return out
 
     def render(self) -> bytes:
-        """renderer.py:209-219: W*H*4 RGBA8 bytes, bottom row first."""
-        return self.render_array().tobytes()
+        """renderer.py:209-219: W*H*4 RGBA8 bytes, bottom row first (copied
+        once, from the handle's page-locked image)."""
+        p = ctypes.c_void_p()
+        check(self._lib.pvr_render_pinned(self._handle(), ctypes.byref(p)))
+        return ctypes.string_at(p.value, self.width * self.height * 4)
 
     def render_float(self):
         """(rgba8, float32 (H, W, 4) pre-blend fragment colour)."""

@@ -174,10 +174,13 @@ def read_vti(file_path: Union[str, Path]) -> Dict:
     return {"dims": dims, "spacing": spacing, "origin": origin, "arrays": arrays, "_payload": payload}
 
 
-def load_vtk_volume(file_path: Union[str, Path], scalars_name: str = "Scalars_") -> Volume:
+def load_vtk_volume(file_path: Union[str, Path], scalars_name: str = "Scalars_",
+                    compute_normals: bool = True) -> Volume:
     """A ``.vti`` file as a Volume, as pyvr/dataloaders/vtk_loader.py:15-146
     builds it (normalised float32 data, aspect-preserving bounds in [-1, 1],
-    name ``file(Scalars)``, normals computed)."""
+    name ``file(Scalars)``, normals computed).  compute_normals=False
+    (extension) leaves the normals to the GPU layout (``DeviceVolume(...,
+    normals="device")``), which gives the same normals."""
     file_path = Path(file_path)
     if not file_path.exists():
         raise FileNotFoundError(f"VTK file not found: {file_path}")
@@ -209,7 +212,8 @@ def load_vtk_volume(file_path: Union[str, Path], scalars_name: str = "Scalars_")
     half = phys * scale / 2.0
     vol = Volume(data=norm, normals=None, min_bounds=-half, max_bounds=+half,
                  name=f"{file_path.name}({scalars_name})")
-    vol.compute_normals()
+    if compute_normals:
+        vol.compute_normals()
     return vol
 
 

@@ -118,3 +118,17 @@ def test_normals_shape_is_checked():
     with VolumeRenderer(16, 16) as r:
         with pytest.raises(ValueError):
             r.load_volume(vol)
+
+
+def test_render_bytes_come_from_the_pinned_image():
+    with VolumeRenderer(40, 24) as r:
+        r.load_volume(_volume(seed=3))
+        r.set_camera(Camera.isometric_view(distance=3.0))
+        r.set_transfer_functions(W.standin_colormap(3), OpacityTransferFunction.linear(0.0, 0.5))
+        a = r.render()
+        assert isinstance(a, bytes) and a == r.render_array().tobytes()
+        r.set_camera(Camera.front_view(distance=3.0))
+        b = r.render()
+        assert b != a and b == r.render_array().tobytes()
+        r.set_camera(Camera.isometric_view(distance=3.0))
+        assert r.render_array().tobytes() == a  # the first result was a copy, not a view

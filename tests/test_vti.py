@@ -60,6 +60,10 @@ def test_volume_semantics(tmp_path):
     assert np.allclose(v.max_bounds, half) and np.allclose(v.min_bounds, -half)
     assert np.isclose(np.abs(v.max_bounds).max(), 1.0)
     assert np.array_equal(v.normals, compute_normal_volume(v.data), equal_nan=True)
+    # normals left to the device layout: same data and bounds, no host normals
+    w = load_vtk_volume(p, compute_normals=False)
+    assert w.normals is None and np.array_equal(w.data, v.data)
+    assert np.array_equal(w.min_bounds, v.min_bounds) and np.array_equal(w.max_bounds, v.max_bounds)
 
 
 def test_constant_volume_and_errors(tmp_path):
