@@ -67,9 +67,13 @@ def parse_args():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="oracle seconds of the CPU baseline")
     ap.add_argument("--probe-s", type=float, default=2.0, help="seconds per rate probe")
-    ap.add_argument("--refine", type=int, default=3, help="bisection probes after the doubling sweep")
-    ap.add_argument("--slots", type=int, default=3, help="server: batches in flight")
-    ap.add_argument("--linger-us", type=int, default=1000, help="server: hold a partial batch this long")
+    ap.add_argument("--refine", type=int, default=4, help="bisection probes after the doubling sweep")
+    ap.add_argument("--slots", type=int, default=8, help="server: launches in flight (streams)")
+    ap.add_argument("--max-batch", type=int, default=64, help="server: requests per launch")
+    ap.add_argument("--batch-pixels", type=int, default=512 * 512,
+                    help="server: pixels per launch (renders this large run as launches of their own, "
+                         "side by side on the slots' streams)")
+    ap.add_argument("--linger-us", type=int, default=0, help="server: hold a partial batch this long")
     ap.add_argument("--serving-brick-log2", type=int, default=4, help="brick size of the resident volumes")
     ap.add_argument("--serving-volumes", type=int, default=32)
     ap.add_argument("--serving-max-dim", type=int, default=512)
@@ -222,7 +226,8 @@ def serving_section(args, torch):
                            max_dim=args.serving_max_dim, seed=0)
     pin_host_volumes(wl, torch)
     # kernel events and sample counters on every 8th batch (the roofline)
-    server = NativeRenderServer(budget_bytes=40 << 30, max_batch=64, slots=args.slots, instrument=8,
+    server = NativeRenderServer(budget_bytes=40 << 30, max_batch=args.max_batch, slots=args.slots, instrument=8,
+                                batch_pixels=args.batch_pixels,
                                 linger_us=args.linger_us, brick_log2=args.serving_brick_log2)
     serial = NativeRenderServer(budget_bytes=40 << 30, per_frame=True, brick_log2=args.serving_brick_log2)
     for slot in range(wl.n_catalog):
@@ -287,16 +292,21 @@ def serving_section(args, torch):
     srv_reqs, srv_el, st, srv_attempts = timed_run(server, r_server, 500)
     ser_reqs, ser_el, _, ser_attempts = timed_run(serial, r_serial, 500)
     clk = clocks.stop()
-    # our kernels in the timed region: batch marches (server), single-render
-    # marches (per-frame), LUT builds of new transfer functions (both)
+    # our kernels in the timed region: the server's marches (one launch per
+    # batch), the per-frame marches, LUT builds of new transfer functions
     launches = (st["batches"] + serial.stats()["batches"] + srv_attempts[-1]["lut_builds"]
                 + ser_attempts[-1]["lut_builds"])
     r_server, r_serial = srv_attempts[-1]["offered"], ser_attempts[-1]["offered"]
-    # roofline of the batch march kernel over the timed steps: algorithmic
-    # bytes of the shaded samples / summed event-timed batch-kernel time
+    # roofline of the server's march over the timed steps: algorithmic bytes
+    # of the shaded samples (measured on every 8th launch, scaled to all
+    # launches) over the timed wall time.  Launches overlap on the device,
+    # so their own event times add up to more than the time the GPU spent;
+    # the wall time includes idle gaps, so this is a lower bound.
     peak, peak_kind = measured_peaks()
     k_ms = st["kernel_ms"]
-    achieved = st["algorithmic_bytes"] / (k_ms / 1000.0) / 1e9 if k_ms else 0.0
+    inst = max(1, st["instrumented_batches"])
+    alg_per_launch = st["algorithmic_bytes"] / inst
+    achieved = alg_per_launch * st["batches"] / srv_el / 1e9
     d2h = sum(r.width * r.height * 4 for r in srv_reqs)
     # uploads: volumes not yet resident (tables of new transfer functions are
     # built on the device from their control points, passed as kernel
@@ -312,17 +322,18 @@ def serving_section(args, torch):
                mean_batch=st["jobs"] / max(1, st["batches"]), max_batch=st["max_jobs"],
                kernel_ms=k_ms, inbox_samples=st["inbox_samples"], shaded_samples=st["shaded_samples"],
                mean_inbox_per_request=st["inbox_samples"] / max(1, st["instrumented_jobs"]),
-               gpu_busy_frac=k_ms * st["batches"] / max(1, st["instrumented_batches"]) / 1000.0 / srv_el,
+               summed_launch_time_over_wall=k_ms * st["batches"] / inst / 1000.0 / srv_el,
                roofline={"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
-                         "traffic": SERVING_DRAM_BYTES_PER_SAMPLE * st["shaded_samples"]
-                         / max(1, st["instrumented_batches"]),
+                         "traffic": SERVING_DRAM_BYTES_PER_SAMPLE * st["shaded_samples"] / inst,
                          "traffic_note": "per launch, scaled from a reduced-catalog ncu capture by samples",
-                         "algorithmic_bytes_per_launch": st["algorithmic_bytes"] / max(1, st["instrumented_batches"]),
-                         "launches_timed": st["instrumented_batches"],
-                         "kernel": "march_batch_kernel",
-                         "note": "batches in flight on different streams may overlap; summed launch "
-                                 "times make this a lower bound"},
+                         "algorithmic_bytes_per_launch": alg_per_launch,
+                         "launches": st["batches"], "launches_instrumented": st["instrumented_batches"],
+                         "mean_launch_ms_overlapped": k_ms / inst,
+                         "kernel": ("march_single_kernel" if st["max_jobs"] <= 1
+                                    else "march_batch_kernel + march_single_kernel"),
+                         "note": "algorithmic bytes of all timed launches over the timed wall time "
+                                 "(idle gaps included: a lower bound); launches overlap on the device"},
                clocks=clk, h2d=h2d / args.steps, d2h=d2h / args.steps, setup_s=setup_s,
                loads=server.cache.loads, evictions=server.cache.evictions,
                lut_hits=server.luts.hits, lut_misses=server.luts.misses, workload=wl)
@@ -705,6 +716,11 @@ def serving_config(args):
             "sustained": f"highest offered rate with p99 <= {P99_MS:.0f} ms and completions >= 0.9x "
                          f"offered, found by an untimed sweep (doubling from {NOMINAL_RATE:.0f} req/s, "
                          f"then {args.refine} bisection probes)",
+            "server": (f"continuous batching over {args.slots} launch slots (streams), "
+                       f"up to {args.max_batch} requests and {args.batch_pixels} pixels per launch, "
+                       f"linger {args.linger_us} us; "
+                       "per-frame baseline: same runtime, one request per launch, each read back "
+                       "before the next"),
             "parallelism": f"replicas x{args.gpus}",
             "l2": "resident volumes (~25 GB) far exceed L2"}
 
@@ -757,7 +773,10 @@ def run_ours(args):
                 "probes": {"server": s["probes_server"], "serial": s["probes_serial"]},
                 "timed_attempts": s["attempts"],
                 "batching": {"batches": s["batches"], "mean_jobs_per_batch": s["mean_batch"],
-                             "max_jobs_per_batch": s["max_batch"], "gpu_busy_frac": s["gpu_busy_frac"],
+                             "max_jobs_per_batch": s["max_batch"],
+                             "summed_launch_time_over_wall": s["summed_launch_time_over_wall"],
+                             "server": {"max_batch": args.max_batch, "slots": args.slots,
+                                        "batch_pixels": args.batch_pixels, "linger_us": args.linger_us},
                              "loads": s["loads"], "evictions": s["evictions"],
                              "lut_builds_timed": s["lut_builds"], "lut_hits": s["lut_hits"],
                              "lut_misses": s["lut_misses"]},

@@ -341,6 +341,8 @@ typedef struct {
     int instrument;             /* N > 0: kernel events and sample counters on every N-th batch */
     int linger_us;              /* with a batch in flight, hold a partial batch up to this long */
     pvr_tuning tuning;          /* tile_w == 0: default */
+    long long batch_pixels;     /* > 0: a batch takes queued requests while their pixels sum to at
+                                   most this (its first request always); 0: max_batch alone limits */
 } pvr_server_config;
 
 typedef struct {

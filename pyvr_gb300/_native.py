@@ -178,7 +178,7 @@ class PvrCompletion(ctypes.Structure):
 class PvrServerConfig(ctypes.Structure):
     """pvr_server_config of include/pyvr_gb300.h."""
     _fields_ = [("max_batch", _I), ("slots", _I), ("per_frame", _I), ("instrument", _I), ("linger_us", _I),
-                ("tuning", PvrTuning)]
+                ("tuning", PvrTuning), ("batch_pixels", _LL)]
 
 
 class PvrServerStats(ctypes.Structure):

@@ -9,11 +9,16 @@
 //    batches were on the GPU join the next batch), computes their camera
 //    matrices, and queues [batch march -> one copy of the slot's image arena
 //    to pinned host memory -> event] on the slot's stream;
-//  * the completer: waits for the slots' events in launch order, copies each
-//    image to its request's host buffer, stamps the completion time and
-//    publishes a completion record, then frees the slot.
-// Up to `slots` batches are in flight, each slot on its own stream, so one
-// batch's read-back overlaps the next batch's march.
+//  * the completer: takes the slots whose work has finished, in the order
+//    they finish (a stream callback behind each slot's read-back hands the
+//    slot over and stamps the completion time), copies each image to its
+//    request's host buffer if it was staged, publishes completion records,
+//    then frees the slot.  A long render does not hold back the slots that
+//    finish after it was launched but before it ends.
+// Up to `slots` batches are in flight, each slot on its own stream: their
+// marches overlap on the device, and one batch's read-back overlaps the next
+// batch's march.  With max_batch = 1 every request is its own launch, and the
+// requests in flight overlap as concurrent kernels.
 //
 // per_frame mode is the per-frame baseline on the same machinery: one slot,
 // one request per launch, and the next launch only after the previous
@@ -53,6 +58,10 @@ struct Req {
 };
 
 struct Slot {
+    pvr_server *srv = nullptr;  // for the completion callback
+    int index = 0;
+    long long t_done = 0;           // set by the completion callback
+    cudaError_t stream_status = cudaSuccess;
     cudaStream_t stream = nullptr;
     pvr_batch *batch = nullptr;
     cudaEvent_t done = nullptr, k0 = nullptr, k1 = nullptr;
@@ -81,7 +90,9 @@ struct pvr_server {
     std::mutex mu;
     std::condition_variable cv_sched, cv_done, cv_poll;
     std::deque<Req> queue;
-    std::deque<int> inflight;  // launched slots, in launch order
+    long long queued_pixels = 0;  // width*height summed over the queue
+    std::deque<int> done_slots;  // slots whose work has finished, in that order
+    int n_inflight = 0;          // launched slots not yet completed
     std::vector<int> free_slots;
     std::deque<pvr_completion> completions;
     bool stop = false;
@@ -143,6 +154,19 @@ void fill_from_request(const pvr_request &r, pvr_job &j) {
     j.max_steps = r.max_steps;
 }
 
+// Stream callback behind a slot's read-back: the slot's work has finished
+// (or the stream has failed).  No CUDA calls are allowed here.
+void CUDART_CB slot_finished(cudaStream_t, cudaError_t status, void *user) {
+    Slot &s = *static_cast<Slot *>(user);
+    s.t_done = now_ns();
+    s.stream_status = status;
+    {
+        std::lock_guard<std::mutex> g(s.srv->mu);
+        s.srv->done_slots.push_back(s.index);
+    }
+    s.srv->cv_done.notify_one();
+}
+
 // the scheduler's half of one batch: returns the status of the launch
 int launch_slot(pvr_server *srv, Slot &s) {
     const int n = (int)s.reqs.size();
@@ -199,6 +223,9 @@ int launch_slot(pvr_server *srv, Slot &s) {
         PVR_CUDA(cudaMemcpyAsync(s.h_arena, s.d_arena, total, cudaMemcpyDeviceToHost, s.stream));
     }
     PVR_CUDA(cudaEventRecord(s.done, s.stream));
+    // last: a failed launch returns before this, and is handed over by the
+    // scheduler instead
+    PVR_CUDA(cudaStreamAddCallback(s.stream, slot_finished, &s, 0));
     return PVR_OK;
 }
 
@@ -215,8 +242,9 @@ void scheduler_loop(pvr_server *srv) {
         }
         // with a batch already on the GPU, a partial batch may wait up to
         // linger_us (from its oldest request's submission) for more requests
-        if (!srv->cfg.per_frame && linger_ns > 0 && !srv->stop && !srv->inflight.empty() &&
-            (int)srv->queue.size() < srv->cfg.max_batch) {
+        if (!srv->cfg.per_frame && linger_ns > 0 && !srv->stop && srv->n_inflight > 0 &&
+            (int)srv->queue.size() < srv->cfg.max_batch &&
+            (srv->cfg.batch_pixels <= 0 || srv->queued_pixels < srv->cfg.batch_pixels)) {
             const long long due = srv->queue.front().t_submit + linger_ns;
             if (now_ns() < due) {
                 srv->cv_sched.wait_until(lk, std::chrono::steady_clock::time_point(std::chrono::nanoseconds(due)));
@@ -225,25 +253,43 @@ void scheduler_loop(pvr_server *srv) {
         }
         const int si = srv->free_slots.back();
         srv->free_slots.pop_back();
+        srv->n_inflight += 1;  // before the launch: its callback may run at once
         Slot &s = srv->slots[si];
         s.reqs.clear();
         const int cap = srv->cfg.per_frame ? 1 : srv->cfg.max_batch;
+        long long px = 0;
         while (!srv->queue.empty() && (int)s.reqs.size() < cap) {
-            s.reqs.push_back(srv->queue.front());
+            const Req &q = srv->queue.front();
+            const long long p = (long long)q.r.width * q.r.height;
+            if (!s.reqs.empty() && srv->cfg.batch_pixels > 0 && px + p > srv->cfg.batch_pixels) break;
+            px += p;
+            srv->queued_pixels -= p;
+            s.reqs.push_back(q);
             srv->queue.pop_front();
         }
         lk.unlock();
         const long long t_launch = now_ns();
         for (auto &q : s.reqs) q.t_launch = t_launch;
-        s.status = launch_slot(srv, s);
-        if (s.status != PVR_OK) {
+        // the slot's fields are written before its completion callback is
+        // queued; a successful launch leaves them untouched afterwards
+        s.stream_status = cudaSuccess;
+        s.status = PVR_OK;
+        const int rc = launch_slot(srv, s);
+        if (rc != PVR_OK) {
+            // whatever part of the batch was queued finishes before the slot
+            // is handed over
             const std::string why = pvr_last_error();
-            std::lock_guard<std::mutex> g(srv->mu);
-            srv->last_error = why;
+            cudaStreamSynchronize(s.stream);
+            s.status = rc;
+            s.t_done = now_ns();
+            {
+                std::lock_guard<std::mutex> g(srv->mu);
+                srv->last_error = why;
+                srv->done_slots.push_back(si);
+            }
+            srv->cv_done.notify_one();
         }
         lk.lock();
-        srv->inflight.push_back(si);
-        srv->cv_done.notify_one();
     }
     srv->sched_exited = true;
     srv->cv_done.notify_all();
@@ -253,20 +299,18 @@ void completer_loop(pvr_server *srv) {
     cudaSetDevice(srv->device);
     std::unique_lock<std::mutex> lk(srv->mu);
     for (;;) {
-        srv->cv_done.wait(lk, [&] { return !srv->inflight.empty() || srv->sched_exited; });
-        if (srv->inflight.empty()) {
-            if (srv->sched_exited) break;
-            continue;
-        }
-        const int si = srv->inflight.front();
+        srv->cv_done.wait(lk, [&] {
+            return !srv->done_slots.empty() || (srv->sched_exited && srv->n_inflight == 0);
+        });
+        if (srv->done_slots.empty()) break;  // the scheduler has exited and nothing is in flight
+        const int si = srv->done_slots.front();
+        srv->done_slots.pop_front();
         lk.unlock();
         Slot &s = srv->slots[si];
         int status = s.status;
-        if (status == PVR_OK) {
-            const cudaError_t e = cudaEventSynchronize(s.done);
-            if (e != cudaSuccess) status = pvr::cuda_fail(e, "batch completion");
-        }
-        const long long t_done = now_ns();
+        if (status == PVR_OK && s.stream_status != cudaSuccess)
+            status = pvr::cuda_fail(s.stream_status, "batch completion");
+        const long long t_done = s.t_done;
         std::vector<pvr_completion> out(s.reqs.size());
         long long inbox = 0, shaded = 0;
         double alg = 0.0;
@@ -301,7 +345,7 @@ void completer_loop(pvr_server *srv) {
         }
         for (auto &c : out) srv->completions.push_back(c);
         s.reqs.clear();
-        srv->inflight.pop_front();
+        srv->n_inflight -= 1;
         srv->free_slots.push_back(si);
         srv->cv_sched.notify_one();
         srv->cv_poll.notify_all();
@@ -333,6 +377,7 @@ int pvr_server_create(const pvr_server_config *cfg, pvr_server **out) {
     *out = nullptr;
     if (cfg->max_batch < 1 || cfg->max_batch > 4096) return fail(PVR_ERR_VALUE, "max_batch must be in 1..4096");
     if (cfg->slots < 1 || cfg->slots > 16) return fail(PVR_ERR_VALUE, "slots must be in 1..16");
+    if (cfg->batch_pixels < 0) return fail(PVR_ERR_VALUE, "batch_pixels must be >= 0");
     pvr_server *srv = new pvr_server();
     srv->cfg = *cfg;
     if (srv->cfg.per_frame) {
@@ -364,6 +409,10 @@ int pvr_server_create(const pvr_server_config *cfg, pvr_server **out) {
         destroy_slots(srv);
         delete srv;
         return rc;
+    }
+    for (int i = 0; i < srv->cfg.slots; ++i) {
+        srv->slots[i].srv = srv;
+        srv->slots[i].index = i;
     }
     for (int i = srv->cfg.slots - 1; i >= 0; --i) srv->free_slots.push_back(i);
     srv->sched = std::thread(scheduler_loop, srv);
@@ -398,6 +447,7 @@ int pvr_server_submit(pvr_server *srv, const pvr_request *req) {
         std::lock_guard<std::mutex> g(srv->mu);
         if (srv->stop) return fail(PVR_ERR_STATE, "server is shutting down");
         srv->queue.push_back(q);
+        srv->queued_pixels += (long long)r.width * r.height;
         srv->stats.submitted += 1;
     }
     srv->cv_sched.notify_one();

@@ -70,14 +70,14 @@ def test_server_with_evictions():
     assert stats["evictions"] > 0
 
 
-def _run_native(budget, n_req=160, per_frame=False, max_batch=16):
+def _run_native(budget, n_req=160, per_frame=False, max_batch=16, slots=3, batch_pixels=0):
     """Results of the native server (batched or per-frame) and of the serial
     Python renderer for the same stream."""
     from pyvr_gb300.server import NativeRenderServer
     wl = _workload()
     stream = wl.requests(rate=4000.0, duration=1.0, seed=3)[:n_req]
-    server = NativeRenderServer(budget_bytes=budget, max_batch=max_batch, slots=3, per_frame=per_frame,
-                                instrument=1)
+    server = NativeRenderServer(budget_bytes=budget, max_batch=max_batch, slots=slots, per_frame=per_frame,
+                                instrument=1, batch_pixels=batch_pixels)
     serial = SerialRenderer()
     for slot in range(wl.n_catalog):
         vol, vs = wl.volumes[slot]
@@ -111,6 +111,40 @@ def test_native_server_results_equal_results_alone(per_frame):
     else:
         assert stats["max_jobs"] == 16  # held requests formed full batches
     assert stats["lat"]["n"] == len(stream)
+
+
+def test_native_server_concurrent_launches_complete_out_of_order():
+    """max_batch=1 over several slots: every request is its own launch, the
+    launches overlap on the device, results equal the results alone, and a
+    short render launched after a long one is handed back when it is done."""
+    from pyvr_gb300 import RenderConfig
+    from pyvr_gb300.server import NativeRenderServer
+    wl, stream, got, want, stats = _run_native(budget=40 << 30, max_batch=1, slots=8)
+    for g, w in zip(got, want):
+        assert g.tobytes() == w
+    assert stats["max_jobs"] == 1 and stats["batches"] == len(stream)
+    server = NativeRenderServer(budget_bytes=1 << 30, max_batch=1, slots=8)
+    vol, vs = wl.volumes[0]
+    server.cache.insert(0, vol, vs, server._free_volume)
+    base = dict(stream[0][1], volume_id=0, kind="render")
+    long = RenderRequest(**dict(base, width=1024, height=1024, config=RenderConfig.ultra_quality()))
+    short = [RenderRequest(**dict(base, width=32, height=32)) for _ in range(6)]
+    server.pause(True)
+    futs = [server.submit(r) for r in [long] + short]
+    server.pause(False)
+    for f in futs:
+        f.result(timeout=60)
+    server.close()
+    assert all(s.launched_at >= long.launched_at for s in short)
+    assert any(s.done_at < long.done_at for s in short), [(s.launched_at, s.done_at) for s in short]
+
+
+def test_native_server_pixel_budget_per_launch():
+    # 48^2 renders pair up within 2 x 48^2 pixels; a 64^2 capture goes alone
+    wl, stream, got, want, stats = _run_native(budget=40 << 30, max_batch=16, batch_pixels=2 * 48 * 48)
+    for g, w in zip(got, want):
+        assert g.tobytes() == w
+    assert stats["max_jobs"] == 2 and stats["jobs"] == len(stream)
 
 
 def test_native_server_with_evictions_and_bad_requests():
