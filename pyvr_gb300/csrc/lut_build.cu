@@ -117,12 +117,14 @@ extern "C" int pvr_lut_build(pvr_lut *l, const double *ctf_x, const double *ctf_
     if (!pvr::sorted_finite(ctf_x, n_ctf) || !pvr::sorted_finite(otf_x, n_otf))
         return fail(PVR_ERR_VALUE, "control point positions must be finite and sorted");
     if (size > l->cap) {
-        cudaDeviceSynchronize();  // a queued batch may still read the old table
-        cudaFree(l->d_lut);
-        cudaFree(l->d_prefix);
-        l->d_lut = nullptr;
-        l->d_prefix = nullptr;
-        l->cap = 0;
+        if (l->d_lut || l->d_prefix) {
+            cudaDeviceSynchronize();  // a queued batch may still read the old table
+            cudaFree(l->d_lut);
+            cudaFree(l->d_prefix);
+            l->d_lut = nullptr;
+            l->d_prefix = nullptr;
+            l->cap = 0;
+        }  // a new table waits for nothing
         PVR_CUDA(cudaMalloc(&l->d_lut, (size_t)size * sizeof(float4)));
         PVR_CUDA(cudaMalloc(&l->d_prefix, (size_t)(size + 1) * sizeof(int)));
         l->cap = size;

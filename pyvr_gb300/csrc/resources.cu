@@ -325,12 +325,14 @@ int pvr_lut_update(pvr_lut *l, const float *rgba, int size) {
     if (!rgba) return fail(PVR_ERR_VALUE, "LUT is NULL");
     if (size <= 0 || size > (1 << 24)) return fail(PVR_ERR_VALUE, "LUT size must be in 1..2^24, got %d", size);
     if (size > l->cap) {
-        cudaDeviceSynchronize();  // a queued batch may still read the old table
-        cudaFree(l->d_lut);
-        cudaFree(l->d_prefix);
-        l->d_lut = nullptr;
-        l->d_prefix = nullptr;
-        l->cap = 0;
+        if (l->d_lut || l->d_prefix) {
+            cudaDeviceSynchronize();  // a queued batch may still read the old table
+            cudaFree(l->d_lut);
+            cudaFree(l->d_prefix);
+            l->d_lut = nullptr;
+            l->d_prefix = nullptr;
+            l->cap = 0;
+        }  // a new table waits for nothing
         PVR_CUDA(cudaMalloc(&l->d_lut, (size_t)size * sizeof(float4)));
         PVR_CUDA(cudaMalloc(&l->d_prefix, (size_t)(size + 1) * sizeof(int)));
         l->cap = size;

@@ -812,13 +812,17 @@ def drive(impl, stream, timeout: float = 300.0):
     if not reqs:
         return reqs, 0.0
     # the request objects (and everything else alive now) are moved out of the
-    # cyclic collector's reach for the replay, so that no collection pause
-    # falls between a request's arrival stamp and its submission
+    # cyclic collector's reach, and the collector is off for the replay (as
+    # in a latency-bound service): no collection pause holds up a submission
     gc.collect()
     gc.freeze()
+    enabled = gc.isenabled()
+    gc.disable()
     try:
         return _replay(impl, stream, reqs, timeout)
     finally:
+        if enabled:
+            gc.enable()
         gc.unfreeze()
 
 
@@ -827,7 +831,9 @@ def _replay(impl, stream, reqs, timeout):
         t0 = time.perf_counter()
         for (off, _), req in zip(stream, reqs):
             _wait_until(t0 + off)
-            req.arrival = time.perf_counter()
+            # the scheduled arrival: a submission that runs late (the client
+            # thread held up) counts against the request's latency
+            req.arrival = t0 + off
             impl.submit(req).add_done_callback(_consume(req))
         for req in reqs:
             req.future.result(timeout=timeout)
@@ -851,7 +857,7 @@ def _replay(impl, stream, reqs, timeout):
     t0 = time.perf_counter()
     for (off, _), req in zip(stream, reqs):
         _wait_until(t0 + off)
-        req.arrival = time.perf_counter()
+        req.arrival = t0 + off
         q.put(req)
     q.put(None)
     for req in reqs:
