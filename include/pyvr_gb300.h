@@ -174,6 +174,15 @@ int pvr_volume_destroy(pvr_volume *v);   /* waits for the whole device first */
  * invalid on return. */
 int pvr_volume_release(pvr_volume *v, void *stream);
 int pvr_volume_device_bytes(const pvr_volume *v, long long *bytes);
+/* Bytes per texel record of the volume's layout: 16 (float value + float
+ * normal) or 8 (the same four floats as halves, used when every one of them
+ * is a half exactly -- float16 volumes with normals computed in half
+ * precision, as numpy does for float16 input).  No reference counterpart:
+ * the GL path keeps voxels and normals in two textures (manager.py:77-135). */
+int pvr_volume_record_bytes(const pvr_volume *v, int *bytes);
+/* Whether layouts built after the call may use 8-byte records (default 1);
+ * either form renders the same images. */
+int pvr_set_compact_records(int enabled);
 /* The float32 (D,H,W,3) normals held in the records (host buffer): what
  * Volume.normals holds after compute_normal_volume (pyvr/volume/data.py:103-118),
  * read back from the device. */

@@ -69,6 +69,13 @@ class DeviceVolume:
         check(_lib().pvr_volume_device_bytes(self.handle, ctypes.byref(n)))
         return int(n.value)
 
+    def record_bytes(self) -> int:
+        """16 (float records) or 8 (half records: every value and normal of
+        the volume is a half exactly)."""
+        n = ctypes.c_int(0)
+        check(_lib().pvr_volume_record_bytes(self.handle, ctypes.byref(n)))
+        return int(n.value)
+
     def read_normals(self) -> np.ndarray:
         out = np.empty(self.shape + (3,), dtype=np.float32)
         check(_lib().pvr_volume_read_normals(self.handle, out.ctypes.data))
@@ -84,6 +91,12 @@ class DeviceVolume:
             self.close()
         except Exception:
             pass
+
+
+def set_compact_records(enabled: bool) -> None:
+    """Allow (default) or forbid 8-byte half records for volumes laid out
+    from now on; either form renders the same images."""
+    check(_lib().pvr_set_compact_records(int(bool(enabled))))
 
 
 class DeviceLUT:

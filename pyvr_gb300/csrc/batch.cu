@@ -20,9 +20,9 @@ namespace pvr {
 const void *batch_kernel_b2(const Tuning &);
 const void *batch_kernel_b3(const Tuning &);
 const void *batch_kernel_b4(const Tuning &);
-const void *single_kernel_b2(const Tuning &);
-const void *single_kernel_b3(const Tuning &);
-const void *single_kernel_b4(const Tuning &);
+const void *single_kernel_b2(const Tuning &, int);
+const void *single_kernel_b3(const Tuning &, int);
+const void *single_kernel_b4(const Tuning &, int);
 int max_batch_blocks_b2(const Tuning &, int);
 int max_batch_blocks_b3(const Tuning &, int);
 int max_batch_blocks_b4(const Tuning &, int);
@@ -35,11 +35,11 @@ const void *batch_kernel(int log2b, const Tuning &t) {
     }
 }
 
-const void *single_kernel(int log2b, const Tuning &t) {
+const void *single_kernel(int log2b, const Tuning &t, int variant) {
     switch (log2b) {
-    case 2: return single_kernel_b2(t);
-    case 4: return single_kernel_b4(t);
-    default: return single_kernel_b3(t);
+    case 2: return single_kernel_b2(t, variant);
+    case 4: return single_kernel_b4(t, variant);
+    default: return single_kernel_b3(t, variant);
     }
 }
 
@@ -155,12 +155,10 @@ int launch_chunk(pvr_batch *b, const pvr_job *jobs, int n, cudaStream_t st) {
     const int log2b = jobs[0].volume->log2b;
     int max_lut = 1;
     for (int i = 0; i < n; ++i) max_lut = std::max(max_lut, jobs[i].lut->size);
-    Slot &s = b->slots[b->next];
-    if (s.pending) {
-        PVR_CUDA(cudaEventSynchronize(s.done));
-        s.pending = false;
-    }
-    if (n == 1) {  // one job: the single-job kernel, one block per tile
+    if (n == 1) {
+        // one job: the single-job kernel of its variant, one block per tile,
+        // launched directly (its parameters are copied at the launch, and it
+        // uses no work counter)
         pvr::SingleParams &sp = b->single;
         if (int rc = pvr::fill_job(jobs[0], b->tuning.tile_w, b->tuning.tile_h, sp.job)) return rc;
         sp.tile_w = b->tuning.tile_w;
@@ -168,23 +166,20 @@ int launch_chunk(pvr_batch *b, const pvr_job *jobs, int n, cudaStream_t st) {
         int lut_smem = 256;
         while (lut_smem < max_lut && lut_smem < 2048) lut_smem *= 2;
         sp.lut_smem_entries = lut_smem;
+        const bool smem = sp.job.f.lut_size <= lut_smem;
+        const int variant = (sp.job.normals ? pvr::kSingleNormals : 0) | (smem ? pvr::kSingleSmemLut : 0) |
+                            (sp.job.compact ? pvr::kSingleCompact : 0);
         const long long tiles = (long long)sp.job.tiles_x * sp.job.tiles_y;
-        LaunchKey key;
-        key.fn = pvr::single_kernel(log2b, b->tuning);
-        key.grid = (int)tiles;
-        key.lut_smem = lut_smem;
         void *args[] = {&sp};
-        if (!s.exec || !(s.key == key)) {
-            if (int rc = build_graph(s, key, args)) return rc;
-        } else {
-            cudaKernelNodeParams kp = kernel_params(key, args);
-            PVR_CUDA(cudaGraphExecKernelNodeSetParams(s.exec, s.kernel_node, &kp));
-        }
-        PVR_CUDA(cudaGraphLaunch(s.exec, st));
-        PVR_CUDA(cudaEventRecord(s.done, st));
-        s.pending = true;
-        b->next = (b->next + 1) % (int)b->slots.size();
+        PVR_CUDA(cudaLaunchKernel(pvr::single_kernel(log2b, b->tuning, variant), dim3((unsigned)tiles),
+                                  dim3(pvr::kBatchThreads), args, smem ? pvr::batch_smem_bytes(lut_smem) : 0,
+                                  st));
         return PVR_OK;
+    }
+    Slot &s = b->slots[b->next];
+    if (s.pending) {
+        PVR_CUDA(cudaEventSynchronize(s.done));
+        s.pending = false;
     }
     pvr::BatchParams &p = *b->params;
     long long total = 0;

@@ -198,12 +198,49 @@ __global__ void brick_minmax_kernel(BrickGeometry g, const uint32_t *__restrict_
     }
 }
 
+// A float survives float -> half -> float bit for bit (NaN: as some NaN).
+__device__ __forceinline__ bool half_exact(float x, unsigned short &h) {
+    const __half hv = __float2half_rn(x);
+    h = __half_as_ushort(hv);
+    const float back = __half2float(hv);
+    if (x != x) return back != back;
+    return __float_as_uint(back) == __float_as_uint(x);
+}
+
+// Compact records: {value, nx, ny, nz} as four halves in one 8-byte record.
+// The march decodes them exactly, so a volume whose records all survive the
+// round trip renders the same images from either form.
+__global__ void compact_records_kernel(const float4 *__restrict__ in, uint2 *__restrict__ out, long long n,
+                                       int *__restrict__ inexact) {
+    bool ok = true;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const float4 r = in[i];
+        unsigned short h0, h1, h2, h3;
+        ok &= half_exact(r.x, h0);
+        ok &= half_exact(r.y, h1);
+        ok &= half_exact(r.z, h2);
+        ok &= half_exact(r.w, h3);
+        out[i] = make_uint2((uint32_t)h0 | ((uint32_t)h1 << 16), (uint32_t)h2 | ((uint32_t)h3 << 16));
+    }
+    if (__any_sync(0xffffffffu, !ok) && (threadIdx.x & 31) == 0) atomicExch(inexact, 1);
+}
+
+__device__ __forceinline__ float4 record_at(const float4 *r, size_t i) { return r[i]; }
+__device__ __forceinline__ float4 record_at(const uint2 *r, size_t i) {
+    const uint2 q = r[i];
+    return make_float4(__half2float(__ushort_as_half((unsigned short)(q.x & 0xffffu))),
+                       __half2float(__ushort_as_half((unsigned short)(q.x >> 16))),
+                       __half2float(__ushort_as_half((unsigned short)(q.y & 0xffffu))),
+                       __half2float(__ushort_as_half((unsigned short)(q.y >> 16))));
+}
+
 // Scatter the normals held in the records back to (D,H,W,3): one thread per
 // texel, reading the record of local index (k+1) % B in brick (k+1) / B.
-template <int LOG2B>
+template <int LOG2B, typename Rec>
 __global__ void read_normals_kernel(BrickGeometry g, int D, int H, int W,
                                     const uint32_t *__restrict__ table,
-                                    const float4 *__restrict__ records, float *__restrict__ out) {
+                                    const Rec *__restrict__ records, float *__restrict__ out) {
     constexpr int B = 1 << LOG2B, A = B + 1, R = A * A * A;
     const long long total = (long long)D * H * W;
     for (long long src = blockIdx.x * (long long)blockDim.x + threadIdx.x; src < total;
@@ -215,7 +252,7 @@ __global__ void read_normals_kernel(BrickGeometry g, int D, int H, int W,
         const int kx = x + 1, ky = y + 1, kz = z + 1;
         const int id = ((kx >> LOG2B) * g.nb[1] + (ky >> LOG2B)) * g.nb[2] + (kz >> LOG2B);
         const int rec = ((kx & (B - 1)) * A + (ky & (B - 1))) * A + (kz & (B - 1));
-        const float4 v = records[(size_t)table[id] * R + rec];
+        const float4 v = record_at(records, (size_t)table[id] * R + rec);
         out[3 * src + 0] = v.y;
         out[3 * src + 1] = v.z;
         out[3 * src + 2] = v.w;
@@ -301,15 +338,30 @@ cudaError_t launch_build_records(const BrickGeometry &g, int dtype, const void *
     }
 }
 
-cudaError_t launch_read_normals(const BrickGeometry &g, const int dims[3], const uint32_t *table,
-                                const float4 *records, float *out, cudaStream_t st) {
-    const long long total = (long long)dims[0] * dims[1] * dims[2];
-    int blocks = (int)std::min<long long>((total + 255) / 256, 152LL * 64);
+template <typename Rec>
+void read_normals_typed(const BrickGeometry &g, const int dims[3], const uint32_t *table, const Rec *records,
+                        float *out, int blocks, cudaStream_t st) {
     switch (g.log2b) {
     case 2: read_normals_kernel<2><<<blocks, 256, 0, st>>>(g, dims[0], dims[1], dims[2], table, records, out); break;
     case 4: read_normals_kernel<4><<<blocks, 256, 0, st>>>(g, dims[0], dims[1], dims[2], table, records, out); break;
     default: read_normals_kernel<3><<<blocks, 256, 0, st>>>(g, dims[0], dims[1], dims[2], table, records, out);
     }
+}
+
+cudaError_t launch_read_normals(const BrickGeometry &g, const int dims[3], const uint32_t *table,
+                                const void *records, bool compact, float *out, cudaStream_t st) {
+    const long long total = (long long)dims[0] * dims[1] * dims[2];
+    int blocks = (int)std::min<long long>((total + 255) / 256, 152LL * 64);
+    if (compact) read_normals_typed(g, dims, table, (const uint2 *)records, out, blocks, st);
+    else read_normals_typed(g, dims, table, (const float4 *)records, out, blocks, st);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_compact_records(const float4 *records, uint2 *out, long long n, int *inexact,
+                                   cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    const int blocks = (int)std::min<long long>((n + 255) / 256, 152LL * 16);
+    compact_records_kernel<<<blocks, 256, 0, st>>>(records, out, n, inexact);
     return cudaGetLastError();
 }
 

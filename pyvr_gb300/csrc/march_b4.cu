@@ -5,7 +5,7 @@ namespace pvr {
 
 const void *batch_kernel_b2(const Tuning &t) { return batch_kernel_log2<2>(t); }
 
-const void *single_kernel_b2(const Tuning &t) { return single_kernel_log2<2>(t); }
+const void *single_kernel_b2(const Tuning &t, int variant) { return single_kernel_log2<2>(t, variant); }
 
 int max_batch_blocks_b2(const Tuning &t, int lut_smem_entries) {
     return max_blocks_log2<2>(t, lut_smem_entries);

@@ -30,6 +30,10 @@
 //    exact: a lerp fmaf(t, b-a, a) with t in [0,1) stays within [a, b], so
 //    a sample lies in the brick's value range, and the scale and the LUT
 //    coordinate are monotone float operations evaluated as for a sample.
+//
+// A volume's records are 16-byte floats, or 8-byte halves when every float
+// of them is a half exactly (layout.cu); the half form decodes to the same
+// floats, so the arithmetic, and every output bit, is the same.
 #pragma once
 
 #include "pvr_device.cuh"
@@ -40,6 +44,24 @@ namespace pvr {
 __device__ __forceinline__ float2 lo2(float4 v) { return make_float2(v.x, v.y); }
 __device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z, v.w); }
 __device__ __forceinline__ float2 dup2(float v) { return make_float2(v, v); }
+
+template <bool COMPACT> struct RecordOf { using T = float4; };
+template <> struct RecordOf<true> { using T = uint2; };
+
+__device__ __forceinline__ float half_lo(uint32_t b) { return __half2float(__ushort_as_half((unsigned short)(b & 0xffffu))); }
+__device__ __forceinline__ float half_hi(uint32_t b) { return __half2float(__ushort_as_half((unsigned short)(b >> 16))); }
+
+// {value, nx, ny, nz} of one record
+__device__ __forceinline__ float4 load_rec(const float4 *p) { return __ldg(p); }
+__device__ __forceinline__ float4 load_rec(const uint2 *p) {
+    const uint2 r = __ldg(p);
+    return make_float4(half_lo(r.x), half_hi(r.x), half_lo(r.y), half_hi(r.y));
+}
+// the stored value of one record
+__device__ __forceinline__ float load_value(const float4 *p) { return __ldg(reinterpret_cast<const float *>(p)); }
+__device__ __forceinline__ float load_value(const uint2 *p) {
+    return __half2float(__ldg(reinterpret_cast<const __half *>(p)));
+}
 
 template <bool SMEM>
 __device__ __forceinline__ float4 lut_entry(const float4 *lut, int i) {
@@ -60,22 +82,22 @@ __device__ __forceinline__ int lut_index(float fl, float lmax, int size) {
 
 // Shading + compositing of one in-box sample (frag:93-115).  p: the record
 // of the footprint's lower corner; fx, fy, fz: the filter fractions.
-template <int LOG2B, bool NORMALS, bool SMEM_LUT>
-__device__ __forceinline__ void shade_sample(const MarchFrame &f, const float4 *__restrict__ p,
+template <int LOG2B, bool NORMALS, bool SMEM_LUT, typename Rec>
+__device__ __forceinline__ void shade_sample(const MarchFrame &f, const Rec *__restrict__ p,
                                              float fx, float fy, float fz, const float4 *lut,
                                              float2 &acc_rg, float2 &acc_ba) {
     constexpr int ROW = brick_apron(LOG2B), SLICE = ROW * ROW;
     float density;
     float n[3];
     if (NORMALS) {
-        const float4 r000 = __ldg(p);
-        const float4 r001 = __ldg(p + 1);
-        const float4 r010 = __ldg(p + ROW);
-        const float4 r011 = __ldg(p + ROW + 1);
-        const float4 r100 = __ldg(p + SLICE);
-        const float4 r101 = __ldg(p + SLICE + 1);
-        const float4 r110 = __ldg(p + SLICE + ROW);
-        const float4 r111 = __ldg(p + SLICE + ROW + 1);
+        const float4 r000 = load_rec(p);
+        const float4 r001 = load_rec(p + 1);
+        const float4 r010 = load_rec(p + ROW);
+        const float4 r011 = load_rec(p + ROW + 1);
+        const float4 r100 = load_rec(p + SLICE);
+        const float4 r101 = load_rec(p + SLICE + 1);
+        const float4 r110 = load_rec(p + SLICE + ROW);
+        const float4 r111 = load_rec(p + SLICE + ROW + 1);
         // texture(volume_texture, tex.zyx) and texture(normal_volume, ...):
         // lerp along z, then y, then x; lanes (value, nx) and (ny, nz)
         const float2 a = lerp_tex2(lerp_tex2(lerp_tex2(lo2(r000), lo2(r001), fz),
@@ -91,11 +113,10 @@ __device__ __forceinline__ void shade_sample(const MarchFrame &f, const float4 *
         n[1] = b.x;
         n[2] = b.y;
     } else {
-        const float *q = reinterpret_cast<const float *>(p);
-        const float v000 = __ldg(q), v001 = __ldg(q + 4);
-        const float v010 = __ldg(q + 4 * ROW), v011 = __ldg(q + 4 * ROW + 4);
-        const float v100 = __ldg(q + 4 * SLICE), v101 = __ldg(q + 4 * SLICE + 4);
-        const float v110 = __ldg(q + 4 * (SLICE + ROW)), v111 = __ldg(q + 4 * (SLICE + ROW) + 4);
+        const float v000 = load_value(p), v001 = load_value(p + 1);
+        const float v010 = load_value(p + ROW), v011 = load_value(p + ROW + 1);
+        const float v100 = load_value(p + SLICE), v101 = load_value(p + SLICE + 1);
+        const float v110 = load_value(p + SLICE + ROW), v111 = load_value(p + SLICE + ROW + 1);
         const float2 zz0 = lerp_tex2(make_float2(v000, v010), make_float2(v001, v011), fz);
         const float2 zz1 = lerp_tex2(make_float2(v100, v110), make_float2(v101, v111), fz);
         const float2 yy = lerp_tex2(make_float2(zz0.x, zz1.x), make_float2(zz0.y, zz1.y), fy);
@@ -173,7 +194,7 @@ __device__ __forceinline__ bool brick_clear(const MarchFrame &f, float2 m, const
 }
 
 // One pixel's ray of volume.frag.glsl:main (lines 70-122).
-template <int LOG2B, int UNROLL, bool NORMALS, bool SMEM_LUT>
+template <int LOG2B, int UNROLL, bool NORMALS, bool SMEM_LUT, bool COMPACT>
 __device__ __forceinline__ void march_ray(const JobDesc &job, int px, int py, const float4 *lut,
                                           const int *prefix, float2 &acc_rg, float2 &acc_ba,
                                           unsigned &n_inbox, unsigned &n_shaded) {
@@ -195,7 +216,8 @@ __device__ __forceinline__ void march_ray(const JobDesc &job, int px, int py, co
     bool entered = false;
     int cur_brick = -1;
     bool clear = false;
-    const float4 *bp = job.records;
+    using Rec = typename RecordOf<COMPACT>::T;
+    const Rec *bp = static_cast<const Rec *>(job.records);
     int i = 0;
     for (;;) {
 #pragma unroll
@@ -219,7 +241,7 @@ __device__ __forceinline__ void march_ray(const JobDesc &job, int px, int py, co
                 if (id != cur_brick) {
                     cur_brick = id;
                     const uint4 bi = __ldg(job.bricks + id);
-                    bp = job.records + (size_t)bi.x * RECS;
+                    bp = static_cast<const Rec *>(job.records) + (size_t)bi.x * RECS;
                     clear = job.skip &&
                             brick_clear<SMEM_LUT>(f, make_float2(__uint_as_float(bi.y), __uint_as_float(bi.z)),
                                                   prefix);
@@ -247,15 +269,15 @@ __device__ __forceinline__ void march_ray(const JobDesc &job, int px, int py, co
     }
 }
 
-template <int LOG2B, int UNROLL, bool NORMALS, bool SMEM_LUT>
+template <int LOG2B, int UNROLL, bool NORMALS, bool SMEM_LUT, bool COMPACT>
 __device__ __forceinline__ void march_tile(const JobDesc &job, int px, int py, const float4 *lut,
                                            const int *prefix, int lane) {
     const bool in_image = px < job.f.width && py < job.f.height;
     float2 acc_rg = make_float2(0.0f, 0.0f), acc_ba = make_float2(0.0f, 0.0f);
     unsigned n_inbox = 0, n_shaded = 0;
     if (in_image)
-        march_ray<LOG2B, UNROLL, NORMALS, SMEM_LUT>(job, px, py, lut, prefix, acc_rg, acc_ba, n_inbox,
-                                                    n_shaded);
+        march_ray<LOG2B, UNROLL, NORMALS, SMEM_LUT, COMPACT>(job, px, py, lut, prefix, acc_rg, acc_ba,
+                                                             n_inbox, n_shaded);
     if (in_image) {
         const long long idx = (long long)py * job.f.width + px;
         if (job.out8) job.out8[idx] = blend_rgba8(acc_rg, acc_ba);
@@ -273,6 +295,27 @@ __device__ __forceinline__ void march_tile(const JobDesc &job, int px, int py, c
             atomicAdd(job.counters + 1, b);
         }
     }
+}
+
+// The job's variant of march_tile: normals or not, LUT staged in shared
+// memory or read from global memory, float or half records.
+template <int LOG2B, int UNROLL, bool COMPACT>
+__device__ __forceinline__ void march_tile_rec(const JobDesc &job, int px, int py, bool lut_in_smem,
+                                               const float4 *s_lut, const int *s_prefix, int lane) {
+    if (job.normals) {
+        if (lut_in_smem) march_tile<LOG2B, UNROLL, true, true, COMPACT>(job, px, py, s_lut, s_prefix, lane);
+        else march_tile<LOG2B, UNROLL, true, false, COMPACT>(job, px, py, job.lut, job.prefix, lane);
+    } else {
+        if (lut_in_smem) march_tile<LOG2B, UNROLL, false, true, COMPACT>(job, px, py, s_lut, s_prefix, lane);
+        else march_tile<LOG2B, UNROLL, false, false, COMPACT>(job, px, py, job.lut, job.prefix, lane);
+    }
+}
+
+template <int LOG2B, int UNROLL>
+__device__ __forceinline__ void march_tile_any(const JobDesc &job, int px, int py, bool lut_in_smem,
+                                               const float4 *s_lut, const int *s_prefix, int lane) {
+    if (job.compact) march_tile_rec<LOG2B, UNROLL, true>(job, px, py, lut_in_smem, s_lut, s_prefix, lane);
+    else march_tile_rec<LOG2B, UNROLL, false>(job, px, py, lut_in_smem, s_lut, s_prefix, lane);
 }
 
 // Persistent batch kernel.  The job table is the kernel's own parameter
@@ -320,20 +363,17 @@ march_batch_kernel(const __grid_constant__ BatchParams p) {
         const int local = t - job.tile_base;
         const int px = (local % job.tiles_x) * p.tile_w + sub_x;
         const int py = (local / job.tiles_x) * p.tile_h + sub_y;
-        if (job.normals) {
-            if (lut_in_smem) march_tile<LOG2B, UNROLL, true, true>(job, px, py, s_lut, s_prefix, lane);
-            else march_tile<LOG2B, UNROLL, true, false>(job, px, py, job.lut, job.prefix, lane);
-        } else {
-            if (lut_in_smem) march_tile<LOG2B, UNROLL, false, true>(job, px, py, s_lut, s_prefix, lane);
-            else march_tile<LOG2B, UNROLL, false, false>(job, px, py, job.lut, job.prefix, lane);
-        }
+        march_tile_any<LOG2B, UNROLL>(job, px, py, lut_in_smem, s_lut, s_prefix, lane);
         __syncthreads();  // s_tile / the staged LUT are rewritten next round
     }
 }
 
 // Single-job kernel: one block per tile of one render; the job descriptor
 // is the parameter block itself (static offsets), as in a plain frame kernel.
-template <int LOG2B, int UNROLL>
+// One instantiation per variant (normals, LUT in shared memory, half
+// records), chosen on the host: each gets its own register allocation.
+// SMEM_LUT requires job.f.lut_size <= p.lut_smem_entries.
+template <int LOG2B, int UNROLL, bool NORMALS, bool SMEM_LUT, bool COMPACT>
 __global__ void __launch_bounds__(kBatchThreads, 5)
 march_single_kernel(const __grid_constant__ SingleParams p) {
     extern __shared__ float4 s_dyn[];
@@ -342,8 +382,7 @@ march_single_kernel(const __grid_constant__ SingleParams p) {
     const JobDesc &job = p.job;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int warps_x = p.tile_w >> 3;
-    const bool lut_in_smem = job.f.lut_size <= p.lut_smem_entries;
-    if (lut_in_smem) {
+    if (SMEM_LUT) {
         for (int k = threadIdx.x; k < job.f.lut_size; k += kBatchThreads) s_lut[k] = job.lut[k];
         for (int k = threadIdx.x; k <= job.f.lut_size; k += kBatchThreads) s_prefix[k] = job.prefix[k];
         __syncthreads();
@@ -351,19 +390,28 @@ march_single_kernel(const __grid_constant__ SingleParams p) {
     const int t = blockIdx.x;
     const int px = (t % job.tiles_x) * p.tile_w + (warp % warps_x) * 8 + (lane & 7);
     const int py = (t / job.tiles_x) * p.tile_h + (warp / warps_x) * 4 + (lane >> 3);
-    if (job.normals) {
-        if (lut_in_smem) march_tile<LOG2B, UNROLL, true, true>(job, px, py, s_lut, s_prefix, lane);
-        else march_tile<LOG2B, UNROLL, true, false>(job, px, py, job.lut, job.prefix, lane);
-    } else {
-        if (lut_in_smem) march_tile<LOG2B, UNROLL, false, true>(job, px, py, s_lut, s_prefix, lane);
-        else march_tile<LOG2B, UNROLL, false, false>(job, px, py, job.lut, job.prefix, lane);
+    march_tile<LOG2B, UNROLL, NORMALS, SMEM_LUT, COMPACT>(job, px, py, SMEM_LUT ? s_lut : job.lut,
+                                                          SMEM_LUT ? s_prefix : job.prefix, lane);
+}
+
+template <int LOG2B, int UNROLL>
+const void *single_variant(int v) {
+    switch (v & 7) {
+    case 0: return (const void *)march_single_kernel<LOG2B, UNROLL, false, false, false>;
+    case 1: return (const void *)march_single_kernel<LOG2B, UNROLL, true, false, false>;
+    case 2: return (const void *)march_single_kernel<LOG2B, UNROLL, false, true, false>;
+    case 3: return (const void *)march_single_kernel<LOG2B, UNROLL, true, true, false>;
+    case 4: return (const void *)march_single_kernel<LOG2B, UNROLL, false, false, true>;
+    case 5: return (const void *)march_single_kernel<LOG2B, UNROLL, true, false, true>;
+    case 6: return (const void *)march_single_kernel<LOG2B, UNROLL, false, true, true>;
+    default: return (const void *)march_single_kernel<LOG2B, UNROLL, true, true, true>;
     }
 }
 
 template <int LOG2B>
-const void *single_kernel_log2(const Tuning &t) {
-    if (t.steps_per_iter >= 4) return (const void *)march_single_kernel<LOG2B, 4>;
-    return (const void *)march_single_kernel<LOG2B, 1>;
+const void *single_kernel_log2(const Tuning &t, int variant) {
+    if (t.steps_per_iter >= 4) return single_variant<LOG2B, 4>(variant);
+    return single_variant<LOG2B, 1>(variant);
 }
 
 template <int LOG2B>

@@ -43,12 +43,17 @@ cudaError_t launch_build_records(const BrickGeometry &g, int dtype, const void *
                                  const float *nrm, int normals_mode, const uint32_t *table,
                                  float4 *records, uint4 *bricks, cudaStream_t st);
 cudaError_t launch_read_normals(const BrickGeometry &g, const int dims[3], const uint32_t *table,
-                                const float4 *records, float *out, cudaStream_t st);
+                                const void *records, bool compact, float *out, cudaStream_t st);
+// Half-precision copy of n records ({value, nx, ny, nz} as four halves, 8
+// bytes); *inexact is set to 1 if some float does not survive the round trip
+// bit for bit (any NaN may stand for any other).
+cudaError_t launch_compact_records(const float4 *records, uint2 *out, long long n, int *inexact,
+                                   cudaStream_t st);
 
 // One render of a batch, as the march kernel reads it.
 struct JobDesc {
     MarchFrame f;
-    const float4 *records;
+    const void *records;  // float4 records, or uint2 (four halves) when compact
     const uint4 *bricks;  // {slot, min bits, max bits, 0} per brick
     const float4 *lut;
     const int *prefix;  // prefix[i] = LUT entries before i that are not exactly clear
@@ -58,7 +63,8 @@ struct JobDesc {
     int tiles_x, tiles_y, tile_base;
     int normals;
     int skip;  // empty-space test on: the LUT has a clear entry and the light terms are finite
-    int pad_[4];
+    int compact;  // 8-byte half records
+    int pad_[3];
 };
 
 // Kernel parameters of one persistent launch: up to kMaxLaunchJobs job
@@ -96,7 +102,9 @@ struct Tuning {
 // Persistent batch march (march_core.cuh), one instantiation per brick size:
 // the kernel function for a tuning, and the blocks of it that fit on an SM.
 const void *batch_kernel(int log2b, const Tuning &t);
-const void *single_kernel(int log2b, const Tuning &t);
+// variant bits of the single-job kernel
+constexpr int kSingleNormals = 1, kSingleSmemLut = 2, kSingleCompact = 4;
+const void *single_kernel(int log2b, const Tuning &t, int variant);
 size_t batch_smem_bytes(int lut_smem_entries);
 int max_batch_blocks_per_sm(int log2b, const Tuning &t, int lut_smem_entries);
 
@@ -118,8 +126,9 @@ struct pvr_volume {
     int normals_mode = 0;     // 0 none, 1 given, 2 computed on the device
     int log2b = pvr::kDefaultBrickLog2;
     pvr::BrickGeometry geo = {};
-    float4 *d_records = nullptr;
+    void *d_records = nullptr;  // float4 records, or uint2 when compact
     size_t records_bytes = 0;
+    bool compact = false;       // records stored as halves (every float survived exactly)
     uint32_t *d_table = nullptr;  // brick -> record slot
     uint4 *d_bricks = nullptr;    // brick -> {slot, min, max}
     bool layout_ready = false;

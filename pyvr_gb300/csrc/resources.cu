@@ -2,6 +2,7 @@
 // pyvr/moderngl_renderer/manager.py:77-135 as bricked texel records) and
 // RGBA LUTs (manager.py:137-186), plus the host-side derivations shared by
 // the renderer and the batch launcher.
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -110,6 +111,10 @@ void free_volume_buffers(pvr_volume *v, cudaStream_t st) {
     v->d_bricks = nullptr;
 }
 
+// Whether layouts built from now on may use 8-byte half records
+// (pvr_set_compact_records).
+static std::atomic<int> g_compact_records{1};
+
 // Records, brick table and value ranges of a volume (once per volume).
 int ensure_volume_layout(pvr_volume *v, cudaStream_t st) {
     if (v->layout_ready) return PVR_OK;
@@ -130,10 +135,36 @@ int ensure_volume_layout(pvr_volume *v, cudaStream_t st) {
     PVR_CUDA(cudaMemcpyAsync(v->d_table, table.data(), table.size() * sizeof(uint32_t),
                              cudaMemcpyHostToDevice, st));
     PVR_CUDA(launch_build_records(v->geo, v->dtype, v->d_vol, v->dims, v->d_nrm, v->normals_mode,
-                                  v->d_table, v->d_records, v->d_bricks, st));
+                                  v->d_table, (float4 *)v->d_records, v->d_bricks, st));
     vol_free(v->d_nrm, st);  // given normals now live in the records
     v->d_nrm = nullptr;
+    // Half records when every value and normal is a half exactly: float16
+    // volumes with normals computed in half precision (numpy's arithmetic
+    // for float16 input) always are, uint8 values are too.  The march reads
+    // half as many bytes per sample and decodes the same floats.
+    uint2 *compact = nullptr;
+    int *d_flag = nullptr;
+    int inexact = 1;
+    v->compact = false;
+    if (g_compact_records.load() && vol_alloc((void **)&compact, nrec * sizeof(uint2), st) == cudaSuccess) {
+        if (vol_alloc((void **)&d_flag, sizeof(int), st) == cudaSuccess &&
+            cudaMemsetAsync(d_flag, 0, sizeof(int), st) == cudaSuccess &&
+            launch_compact_records((const float4 *)v->d_records, compact, (long long)nrec, d_flag, st) ==
+                cudaSuccess)
+            cudaMemcpyAsync(&inexact, d_flag, sizeof(int), cudaMemcpyDeviceToHost, st);
+    }
+    cudaGetLastError();  // a failed allocation or launch above only means: keep the float records
     PVR_CUDA(cudaStreamSynchronize(st));  // `table` leaves scope; ready for any stream
+    vol_free(d_flag, st);
+    if (compact && inexact == 0) {
+        vol_free(v->d_records, st);
+        v->d_records = compact;
+        v->records_bytes = nrec * sizeof(uint2);
+        v->compact = true;
+    } else {
+        vol_free(compact, st);
+    }
+    PVR_CUDA(cudaStreamSynchronize(st));
     v->layout_ready = true;
     return PVR_OK;
 }
@@ -178,6 +209,7 @@ int fill_job(const pvr_job &j, int tile_w, int tile_h, JobDesc &out) {
     f.lut_size = j.lut->size;
     f.flut_size = (float)j.lut->size;
     out.records = v.d_records;
+    out.compact = v.compact ? 1 : 0;
     out.bricks = v.d_bricks;
     out.lut = j.lut->d_lut;
     out.prefix = j.lut->d_prefix;
@@ -286,6 +318,18 @@ int pvr_volume_release(pvr_volume *v, void *stream) {
     return PVR_OK;
 }
 
+int pvr_set_compact_records(int enabled) {
+    pvr::g_compact_records.store(enabled ? 1 : 0);
+    return PVR_OK;
+}
+
+int pvr_volume_record_bytes(const pvr_volume *v, int *bytes) {
+    if (!v || !bytes) return fail(PVR_ERR_VALUE, "NULL argument");
+    if (!v->layout_ready) return fail(PVR_ERR_STATE, "volume layout not built");
+    *bytes = v->compact ? (int)sizeof(uint2) : (int)sizeof(float4);
+    return PVR_OK;
+}
+
 int pvr_volume_device_bytes(const pvr_volume *v, long long *bytes) {
     if (!v || !bytes) return fail(PVR_ERR_VALUE, "NULL argument");
     *bytes = (long long)(v->vol_bytes + v->records_bytes +
@@ -299,7 +343,7 @@ int pvr_volume_read_normals(const pvr_volume *v, float *normals_out) {
     const size_t n = (size_t)v->dims[0] * v->dims[1] * v->dims[2] * 3;
     float *d = nullptr;
     PVR_CUDA(cudaMalloc(&d, n * sizeof(float)));
-    cudaError_t e = pvr::launch_read_normals(v->geo, v->dims, v->d_table, v->d_records, d, 0);
+    cudaError_t e = pvr::launch_read_normals(v->geo, v->dims, v->d_table, v->d_records, v->compact, d, 0);
     if (e == cudaSuccess) e = cudaMemcpy(normals_out, d, n * sizeof(float), cudaMemcpyDeviceToHost);
     cudaFree(d);
     if (e != cudaSuccess) return pvr::cuda_fail(e, "read normals");
