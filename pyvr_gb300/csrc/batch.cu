@@ -155,10 +155,15 @@ int launch_chunk(pvr_batch *b, const pvr_job *jobs, int n, cudaStream_t st) {
     const int log2b = jobs[0].volume->log2b;
     int max_lut = 1;
     for (int i = 0; i < n; ++i) max_lut = std::max(max_lut, jobs[i].lut->size);
+    Slot &s = b->slots[b->next];
+    if (s.pending) {
+        PVR_CUDA(cudaEventSynchronize(s.done));
+        s.pending = false;
+    }
     if (n == 1) {
         // one job: the single-job kernel of its variant, one block per tile,
         // launched directly (its parameters are copied at the launch, and it
-        // uses no work counter)
+        // uses no work counter); the slot's event tracks it like a batch
         pvr::SingleParams &sp = b->single;
         if (int rc = pvr::fill_job(jobs[0], b->tuning.tile_w, b->tuning.tile_h, sp.job)) return rc;
         sp.tile_w = b->tuning.tile_w;
@@ -174,12 +179,10 @@ int launch_chunk(pvr_batch *b, const pvr_job *jobs, int n, cudaStream_t st) {
         PVR_CUDA(cudaLaunchKernel(pvr::single_kernel(log2b, b->tuning, variant), dim3((unsigned)tiles),
                                   dim3(pvr::kBatchThreads), args, smem ? pvr::batch_smem_bytes(lut_smem) : 0,
                                   st));
+        PVR_CUDA(cudaEventRecord(s.done, st));
+        s.pending = true;
+        b->next = (b->next + 1) % (int)b->slots.size();
         return PVR_OK;
-    }
-    Slot &s = b->slots[b->next];
-    if (s.pending) {
-        PVR_CUDA(cudaEventSynchronize(s.done));
-        s.pending = false;
     }
     pvr::BatchParams &p = *b->params;
     long long total = 0;
