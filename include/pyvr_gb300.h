@@ -180,8 +180,10 @@ int pvr_volume_device_bytes(const pvr_volume *v, long long *bytes);
  * precision, as numpy does for float16 input).  No reference counterpart:
  * the GL path keeps voxels and normals in two textures (manager.py:77-135). */
 int pvr_volume_record_bytes(const pvr_volume *v, int *bytes);
-/* Whether layouts built after the call may use 8-byte records (default 1);
- * either form renders the same images. */
+/* Whether layouts built after the call may use 8-byte records (default 0:
+ * off).  Either form renders the same images; half records halve the
+ * records' memory, cost decode instructions per sample, and pay only where
+ * the march waits on memory (large volumes). */
 int pvr_set_compact_records(int enabled);
 /* The float32 (D,H,W,3) normals held in the records (host buffer): what
  * Volume.normals holds after compute_normal_volume (pyvr/volume/data.py:103-118),

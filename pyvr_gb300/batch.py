@@ -94,8 +94,10 @@ class DeviceVolume:
 
 
 def set_compact_records(enabled: bool) -> None:
-    """Allow (default) or forbid 8-byte half records for volumes laid out
-    from now on; either form renders the same images."""
+    """Allow or forbid (default) 8-byte half records for volumes laid out
+    from now on.  Either form renders the same images; half records halve
+    the records' memory of float16 volumes and pay in speed only where the
+    march waits on memory (large volumes)."""
     check(_lib().pvr_set_compact_records(int(bool(enabled))))
 
 

@@ -48,14 +48,19 @@ __device__ __forceinline__ float2 dup2(float v) { return make_float2(v, v); }
 template <bool COMPACT> struct RecordOf { using T = float4; };
 template <> struct RecordOf<true> { using T = uint2; };
 
-__device__ __forceinline__ float half_lo(uint32_t b) { return __half2float(__ushort_as_half((unsigned short)(b & 0xffffu))); }
-__device__ __forceinline__ float half_hi(uint32_t b) { return __half2float(__ushort_as_half((unsigned short)(b >> 16))); }
+// two halves (low, high) of a 32-bit word as floats, in one conversion
+__device__ __forceinline__ float2 half_pair(uint32_t b) {
+    __half2 h;
+    memcpy(&h, &b, sizeof(h));
+    return __half22float2(h);
+}
 
 // {value, nx, ny, nz} of one record
 __device__ __forceinline__ float4 load_rec(const float4 *p) { return __ldg(p); }
 __device__ __forceinline__ float4 load_rec(const uint2 *p) {
     const uint2 r = __ldg(p);
-    return make_float4(half_lo(r.x), half_hi(r.x), half_lo(r.y), half_hi(r.y));
+    const float2 a = half_pair(r.x), b = half_pair(r.y);
+    return make_float4(a.x, a.y, b.x, b.y);
 }
 // the stored value of one record
 __device__ __forceinline__ float load_value(const float4 *p) { return __ldg(reinterpret_cast<const float *>(p)); }

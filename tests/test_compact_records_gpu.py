@@ -18,23 +18,23 @@ torch = pytest.importorskip("torch")
 
 
 @pytest.fixture
-def float_records():
-    set_compact_records(False)
-    yield
+def half_records():
     set_compact_records(True)
+    yield
+    set_compact_records(False)
 
 
 def _both(scenes, **kw):
-    half = _run_batch(scenes, **kw)
-    set_compact_records(False)
+    set_compact_records(True)
     try:
-        full = _run_batch(scenes, **kw)
+        half = _run_batch(scenes, **kw)
     finally:
-        set_compact_records(True)
+        set_compact_records(False)
+    full = _run_batch(scenes, **kw)
     return half, full
 
 
-def test_record_form_follows_exactness():
+def test_record_form_follows_exactness(half_records):
     base = W.value_noise((12, 14, 16), seed=21)
     cases = {
         ("f16", "device"): 8, ("f16", "none"): 8, ("u8", "none"): 8, ("u8", "device"): 16,
@@ -55,7 +55,7 @@ def test_record_form_follows_exactness():
     assert DeviceVolume(Volume(data=data, normals=nrm), normals="given").record_bytes() == 16
 
 
-def test_compaction_can_be_switched_off(float_records):
+def test_float_records_by_default():
     data = W.to_storage(W.value_noise((10, 10, 10), seed=2), "f16")
     assert DeviceVolume(Volume(data=data), normals="device").record_bytes() == 16
 
