@@ -50,11 +50,12 @@ DTYPES = ("u8", "f16", "f32")
 RES = 1024
 N_VOL = 256
 NOMINAL_RATE = 400.0
-# DRAM bytes per in-box sample of the batch march kernel on the serving mix
-# (ncu, 3 launches of a 4-volume serving case: 98.8 MB for about 32.7 M
-# samples) and DRAM bytes of one 1024^2 high_quality f32 frame of the plain
-# workload (ncu, one launch): the traffic estimates of the roofline entries
-SERVING_DRAM_BYTES_PER_SAMPLE = 3.0
+# DRAM bytes per in-box sample of the single-render march kernel on the
+# serving mix (ncu, 3 launches of a 4-volume serving case: 87.0 MB for about
+# 17.9 M samples) and DRAM bytes of one 1024^2 high_quality f32 frame of the
+# plain workload (ncu, one launch): the traffic estimates of the roofline
+# entries
+SERVING_DRAM_BYTES_PER_SAMPLE = 4.9
 PLAIN_F32_DRAM_BYTES_PER_FRAME = 100.4e6
 P99_MS = 20.0
 
