@@ -111,52 +111,61 @@ def measured_peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks/throttle sampling during the timed region."""
+    """nvidia-smi clocks/throttle sampling during the timed region (one or
+    more start/pause intervals, summarised by stop)."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    NAMES = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
 
     def __init__(self, gpu_index):
         self.gpu_index = gpu_index
         self.proc = None
-        self.path = tempfile.mktemp(prefix="pvr_clocks_", suffix=".csv")
+        self.available = True
+        self.sm, self.smax, self.reasons = [], None, set()
 
     def start(self):
+        self.path = tempfile.mktemp(prefix="pvr_clocks_", suffix=".csv")
         try:
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
                                           "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+            self.available = False
 
-    def stop(self):
+    def pause(self):
         if self.proc is None:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+            return
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
+        self.proc = None
         self.fh.close()
-        sm, smax, reasons = [], None, set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         with open(self.path) as f:
             for line in f:
                 parts = [p.strip() for p in line.split(",")]
                 if len(parts) < 9 or not parts[0].isdigit() or int(parts[0]) != self.gpu_index:
                     continue
                 try:
-                    sm.append(float(parts[1]))
-                    smax = float(parts[2])
+                    self.sm.append(float(parts[1]))
+                    self.smax = float(parts[2])
                 except ValueError:
                     continue
-                for n, v in zip(names, parts[5:9]):
+                for n, v in zip(self.NAMES, parts[5:9]):
                     if v.lower().startswith("active"):
-                        reasons.add(n)
+                        self.reasons.add(n)
         os.unlink(self.path)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
-                "reasons": sorted(reasons), "samples": len(sm)}
+
+    def stop(self):
+        self.pause()
+        if not self.available:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        return {"sm_mhz": statistics.median(self.sm) if self.sm else None, "sm_max_mhz": self.smax,
+                "reasons": sorted(self.reasons), "samples": len(self.sm)}
 
 
 def gpu_index(local_rank):
@@ -218,7 +227,9 @@ def pin_host_volumes(workload, torch):
 
 def serving_section(args, torch):
     """The batched server and the per-frame baseline, both on the native
-    serving runtime (pvr_server_*), over the same resident volumes."""
+    serving runtime (pvr_server_*), each measured alone: its own runtime and
+    its own resident copies of the same volumes, closed before the other arm
+    starts, over the same request streams."""
     from pyvr_gb300 import workloads as W
     from pyvr_gb300.replicas import barrier
     from pyvr_gb300.server import NativeRenderServer, drive, latency_stats, sustained_rate
@@ -226,47 +237,11 @@ def serving_section(args, torch):
     wl = W.ServingWorkload(n_volumes=args.serving_volumes, n_extra=args.serving_extra, min_dim=128,
                            max_dim=args.serving_max_dim, seed=0)
     pin_host_volumes(wl, torch)
-    # kernel events and sample counters on every 8th batch (the roofline)
-    server = NativeRenderServer(budget_bytes=40 << 30, max_batch=args.max_batch, slots=args.slots, instrument=8,
-                                batch_pixels=args.batch_pixels,
-                                linger_us=args.linger_us, brick_log2=args.serving_brick_log2)
-    serial = NativeRenderServer(budget_bytes=40 << 30, per_frame=True, brick_log2=args.serving_brick_log2)
-    for slot in range(wl.n_catalog):
-        vol, vs = wl.volumes[slot]
-        server.cache.insert(slot, vol, vs, server._free_volume)
-        serial.cache.insert(slot, vol, vs, serial._free_volume)
-    torch.cuda.synchronize()
+    start = wl.snapshot()
     setup_s = time.perf_counter() - t_setup
-    # warm-up: W untimed one-second segments at the nominal rate, each impl
-    for w in range(args.warmup):
-        drive(server, wl.requests(NOMINAL_RATE, 1.0, 100 + w))
-        drive(serial, wl.requests(NOMINAL_RATE, 1.0, 150 + w))
-    # the workload's state (catalog churn, orbits, TF edits) evolves with every
-    # stream: each measurement below restarts from this point, so that all
-    # of them see the same mix
-    snap = wl.snapshot()
-    reset = lambda: wl.restore(snap)  # noqa: E731
-    # latency at the nominal rate, both (reported, untimed)
-    nom = {}
-    for name, impl in (("server", server), ("serial", serial)):
-        reset()
-        reqs, el = drive(impl, wl.requests(NOMINAL_RATE, 3.0, 200))
-        st = latency_stats(reqs)
-        st["completed_per_s"] = len(reqs) / el
-        nom[name] = st
-    # untimed sweep: highest rate with p99 <= 20 ms (a failing probe is
-    # repeated once)
-    rates = [NOMINAL_RATE * (2 ** k) for k in range(8)]
-    r_server, probes_server = sustained_rate(server, wl, rates, args.probe_s, 300, refine=args.refine,
-                                             reset=reset)
-    r_serial, probes_serial = sustained_rate(serial, wl, rates, args.probe_s, 300, refine=args.refine,
-                                             reset=reset)
-    r_server = r_server or NOMINAL_RATE
-    r_serial = r_serial or NOMINAL_RATE
-    # timed: K one-second steps at the sustained rate, server then serial
     clocks = ClockSampler(gpu_index(dist_env()[2]))
-    clocks.start()
-    def timed_run(impl, rate, seed):
+
+    def timed_run(impl, rate, seed, reset):
         """K one-second steps at `rate`; a run whose p99 exceeds the bound is
         repeated at 0.9x the rate (at most 3 times), so that the reported
         rate is one served within the bound."""
@@ -278,8 +253,10 @@ def serving_section(args, torch):
             m0 = impl.luts.misses
             up0 = impl.cache.uploaded_bytes
             reset()
+            clocks.start()
             reqs, el = drive(impl, wl.requests(rate, float(args.steps), seed))
             torch.cuda.synchronize()
+            clocks.pause()
             barrier()
             lat = latency_stats(reqs)
             attempts.append({"offered": rate, "completed_per_s": len(reqs) / el, "p99_ms": lat.get("p99_ms"),
@@ -290,12 +267,57 @@ def serving_section(args, torch):
             rate *= 0.9
         return reqs, el, impl.stats(), attempts
 
-    srv_reqs, srv_el, st, srv_attempts = timed_run(server, r_server, 500)
-    ser_reqs, ser_el, _, ser_attempts = timed_run(serial, r_serial, 500)
+    def measure(impl, warm_seed):
+        """Warm-up, the latency at the nominal rate, the untimed rate sweep and
+        the timed steps of one implementation."""
+        wl.restore(start)
+        for slot in range(wl.n_catalog):
+            vol, vs = wl.volumes[slot]
+            impl.cache.insert(slot, vol, vs, impl._free_volume)
+        torch.cuda.synchronize()
+        # warm-up: W untimed one-second segments at the nominal rate (the same
+        # streams for both implementations)
+        for w in range(args.warmup):
+            drive(impl, wl.requests(NOMINAL_RATE, 1.0, warm_seed + w))
+        # the workload's state (catalog churn, orbits, TF edits) evolves with
+        # every stream: each measurement below restarts from this point, so
+        # that all of them see the same mix
+        snap = wl.snapshot()
+        reset = lambda: wl.restore(snap)  # noqa: E731
+        reset()
+        reqs, el = drive(impl, wl.requests(NOMINAL_RATE, 3.0, 200))
+        nominal = latency_stats(reqs)
+        nominal["completed_per_s"] = len(reqs) / el
+        # untimed sweep: highest rate with p99 <= 20 ms (a failing probe is
+        # repeated once)
+        rates = [NOMINAL_RATE * (2 ** k) for k in range(8)]
+        rate, probes = sustained_rate(impl, wl, rates, args.probe_s, 300, refine=args.refine, reset=reset)
+        reqs, el, st, attempts = timed_run(impl, rate or NOMINAL_RATE, 500, reset)
+        return dict(nominal=nominal, probes=probes, reqs=reqs, el=el, stats=st, attempts=attempts,
+                    loads=impl.cache.loads, evictions=impl.cache.evictions, lut_hits=impl.luts.hits,
+                    lut_misses=impl.luts.misses)
+
+    # kernel events and sample counters on every 8th launch (the roofline);
+    # the clocks are sampled during the timed steps of both
+    server = NativeRenderServer(budget_bytes=40 << 30, max_batch=args.max_batch, slots=args.slots, instrument=8,
+                                batch_pixels=args.batch_pixels,
+                                linger_us=args.linger_us, brick_log2=args.serving_brick_log2)
+    srv = measure(server, 100)
+    server.close()
+    del server
+    torch.cuda.synchronize()
+    serial = NativeRenderServer(budget_bytes=40 << 30, per_frame=True, brick_log2=args.serving_brick_log2)
+    ser = measure(serial, 100)
+    serial.close()
+    del serial
     clk = clocks.stop()
+    srv_reqs, srv_el, st, srv_attempts = srv["reqs"], srv["el"], srv["stats"], srv["attempts"]
+    ser_reqs, ser_el, ser_attempts = ser["reqs"], ser["el"], ser["attempts"]
+    nom = {"server": srv["nominal"], "serial": ser["nominal"]}
+    probes_server, probes_serial = srv["probes"], ser["probes"]
     # our kernels in the timed region: the server's marches (one launch per
     # batch), the per-frame marches, LUT builds of new transfer functions
-    launches = (st["batches"] + serial.stats()["batches"] + srv_attempts[-1]["lut_builds"]
+    launches = (st["batches"] + ser["stats"]["batches"] + srv_attempts[-1]["lut_builds"]
                 + ser_attempts[-1]["lut_builds"])
     r_server, r_serial = srv_attempts[-1]["offered"], ser_attempts[-1]["offered"]
     # roofline of the server's march over the timed steps: algorithmic bytes
@@ -336,10 +358,8 @@ def serving_section(args, torch):
                          "note": "algorithmic bytes of all timed launches over the timed wall time "
                                  "(idle gaps included: a lower bound); launches overlap on the device"},
                clocks=clk, h2d=h2d / args.steps, d2h=d2h / args.steps, setup_s=setup_s,
-               loads=server.cache.loads, evictions=server.cache.evictions,
-               lut_hits=server.luts.hits, lut_misses=server.luts.misses, workload=wl)
-    server.close()
-    serial.close()
+               loads=srv["loads"], evictions=srv["evictions"],
+               lut_hits=srv["lut_hits"], lut_misses=srv["lut_misses"], workload=wl)
     return out
 
 

@@ -109,6 +109,16 @@ class VolumeCache:
         with self._lock:
             self._users[vid] -= 1
 
+    def clear(self) -> None:
+        """Free every resident volume (nothing may be in flight)."""
+        with self._lock:
+            vols = list(self._vols.values())
+            self._vols.clear()
+            self._bytes.clear()
+            self._users.clear()
+        for dv in vols:
+            dv.close()
+
     def _evict_for(self, need: int, release_after) -> None:
         while self.used + need > self.budget:
             victim = next((k for k in self._vols if self._users.get(k, 0) == 0), None)
@@ -214,6 +224,21 @@ class LutCache:
 
     def release(self, key) -> None:
         self._users[key] -= 1
+
+    def reserve(self, size: int, count: int) -> None:
+        """Allocate ``count`` tables of ``size`` entries up front, so that new
+        transfer functions are built into memory that already exists."""
+        for _ in range(count):
+            self._free.put(size, DeviceLUT(rgba=np.zeros((size, 4), np.float32)))
+
+    def clear(self) -> None:
+        """Free every table (nothing may be in flight)."""
+        luts = list(self._luts.values()) + [l for lst in self._free._free.values() for l in lst]
+        self._luts.clear()
+        self._users.clear()
+        self._free._free.clear()
+        for lut in luts:
+            lut.close()
 
     def _evict(self) -> None:
         while len(self._luts) >= self.capacity:
@@ -587,16 +612,19 @@ class NativeRenderServer:
     into one persistent launch, while renders of that size or larger run as
     launches of their own (the single-render kernel) side by side.  The
     defaults (8 slots, 512^2 pixels per launch) measured best on a mixed
-    512^2 / 1024^2 stream."""
+    512^2 / 1024^2 stream.  ``lut_reserve`` tables of 256 entries are
+    allocated at start, so that new transfer functions are built into
+    existing memory.  close() frees the resident volumes and tables."""
 
     def __init__(self, budget_bytes: int = 40 << 30, max_batch: int = 64, slots: int = 8,
                  tuning: Optional[Tuning] = None, brick_log2: int = 3, loaders: int = 2,
                  instrument: int = 0, per_frame: bool = False, linger_us: int = 0,
-                 batch_pixels: int = 512 * 512):
+                 batch_pixels: int = 512 * 512, lut_reserve: int = 1024):
         import torch
         self.torch = torch
         self.cache = VolumeCache(budget_bytes, brick_log2)
         self.luts = LutCache()
+        self.luts.reserve(256, lut_reserve)
         self.per_frame = per_frame
         self._lut_stream = torch.cuda.Stream()
         self._release_stream = torch.cuda.Stream()
@@ -656,6 +684,9 @@ class NativeRenderServer:
         h, self._h = self._h, None
         self._lib.pvr_server_destroy(h)
         self.torch.cuda.synchronize()
+        self.cache.clear()
+        with self._lock:
+            self.luts.clear()
 
     # -- internals -----------------------------------------------------------------
     def _free_volume(self, dv: DeviceVolume) -> None:
