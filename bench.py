@@ -92,6 +92,8 @@ def parse_args():
                     help="plain section: RenderConfig preset")
     ap.add_argument("--cameras", type=int, default=16)
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--half-records", action="store_true",
+                    help="lay volumes out with 8-byte half records where they are exact")
     ap.add_argument("--skip-e2e", action="store_true")
     return ap.parse_args()
 
@@ -750,6 +752,9 @@ def run_ours(args):
     import torch
     rank, world, local_rank = dist_env()
     torch.cuda.set_device(local_rank)
+    if args.half_records:
+        from pyvr_gb300.batch import set_compact_records
+        set_compact_records(True)
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))

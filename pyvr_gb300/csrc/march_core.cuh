@@ -377,9 +377,11 @@ march_batch_kernel(const __grid_constant__ BatchParams p) {
 // is the parameter block itself (static offsets), as in a plain frame kernel.
 // One instantiation per variant (normals, LUT in shared memory, half
 // records), chosen on the host: each gets its own register allocation.
-// SMEM_LUT requires job.f.lut_size <= p.lut_smem_entries.
+// SMEM_LUT requires job.f.lut_size <= p.lut_smem_entries.  Half records
+// need 16 fewer registers for a sample's 8 records: those variants run 6
+// blocks per SM (40 registers) instead of 5 (48).
 template <int LOG2B, int UNROLL, bool NORMALS, bool SMEM_LUT, bool COMPACT>
-__global__ void __launch_bounds__(kBatchThreads, 5)
+__global__ void __launch_bounds__(kBatchThreads, COMPACT ? 6 : 5)
 march_single_kernel(const __grid_constant__ SingleParams p) {
     extern __shared__ float4 s_dyn[];
     float4 *s_lut = s_dyn;
