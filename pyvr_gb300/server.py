@@ -233,10 +233,9 @@ class LutCache:
 
     def clear(self) -> None:
         """Free every table (nothing may be in flight)."""
-        luts = list(self._luts.values()) + [l for lst in self._free._free.values() for l in lst]
+        luts = list(self._luts.values()) + self._free.drain()
         self._luts.clear()
         self._users.clear()
-        self._free._free.clear()
         for lut in luts:
             lut.close()
 
@@ -284,6 +283,12 @@ class _Pool:
 
     def put(self, key, obj):
         self._free[key].append(obj)
+
+    def drain(self) -> list:
+        """Every free object, removed from the pool."""
+        out = [o for lst in self._free.values() for o in lst]
+        self._free.clear()
+        return out
 
 
 class PyRenderServer:
