@@ -634,6 +634,61 @@ def loaders_section(args, torch):
     return out
 
 
+def c1_section(args, torch):
+    """The small plain case (64^3 float32 double sphere, 256^2, balanced):
+    device-timed frames, frames through render(), and the oracle on all host
+    cores."""
+    from pyvr_gb300 import VolumeRenderer, _native
+    from pyvr_gb300 import workloads as W
+    from pyvr_gb300.renderer import rgba_lut
+    c = W.config_small()
+    w, h = c["width"], c["height"]
+    lib = _native.load()
+    stream = torch.cuda.Stream()
+    sptr = ctypes.c_void_p(stream.cuda_stream)
+    out = torch.empty(w * h * 4, dtype=torch.uint8, device="cuda")
+    frames = 200
+    with VolumeRenderer(w, h, config=c["config"], light=c["light"]) as r:
+        r.load_volume(c["volume"])
+        r.set_camera(c["camera"])
+        r.set_transfer_functions(c["ctf"], c["otf"])
+        for _ in range(max(args.warmup, 3) * 10):
+            _native.check(lib.pvr_render_device(r._h, ctypes.c_void_p(out.data_ptr()), None, sptr))
+        n_samples = r.last_sample_count()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(frames):
+            _native.check(lib.pvr_render_device(r._h, ctypes.c_void_p(out.data_ptr()), None, sptr))
+        b.record(stream)
+        torch.cuda.synchronize()
+        dev_ms = a.elapsed_time(b) / frames
+        for _ in range(10):
+            r.render()
+        t = time.perf_counter()
+        for _ in range(frames):
+            r.set_camera(c["camera"])
+            r.render()
+        e2e_ms = 1000.0 * (time.perf_counter() - t) / frames
+    res = {"ms_per_frame": dev_ms, "frames_per_s": 1000.0 / dev_ms, "e2e_frames_per_s": 1000.0 / e2e_ms,
+           "samples_per_frame": n_samples,
+           "config": "64^3 float32 double sphere, 256x256, balanced, directional light, linear opacity 0-0.1",
+           "note": "L2-resident: a latency figure, not a bandwidth one"}
+    if not args.skip_cpu:
+        import oracle
+        oracle.build()
+        s = W.frame_inputs(c["volume"], c["camera"], c["light"], c["config"], rgba_lut(c["ctf"], c["otf"]),
+                           w, h, c["value_scale"])
+        oracle.render(s, want_float=False)
+        reps = 10
+        t = time.perf_counter()
+        for _ in range(reps):
+            oracle.render(s, want_float=False)
+        cpu_ms = 1000.0 * (time.perf_counter() - t) / reps
+        res["cpu_baseline"] = {"ms_per_frame": cpu_ms, "cores": oracle.max_threads(), "kind": "port",
+                               "gpu_speedup_device": cpu_ms / dev_ms, "gpu_speedup_e2e": cpu_ms / e2e_ms}
+    return res
+
+
 def plain_section(args, torch):
     from pyvr_gb300 import VolumeRenderer, _native
     n_vol, res = args.plain_volume, args.plain_res
@@ -708,10 +763,33 @@ def plain_section(args, torch):
     for dt in rend:
         ms = [m for d, _, m in launch_ms if d == dt]
         by = sum(shaded[(d, k)] * BYTES_PER_SAMPLE[d] for d, k, _ in launch_ms if d == dt)
+        # compulsory bytes: every voxel and its float32x3 normal read once, and
+        # the image written once (an upper bound on what a frame must touch)
+        data = scenes[dt]["volume"].data
+        compulsory = data.size * (data.itemsize + 12) + res * res * 4
         per_dtype[dt] = {"avg_launch_ms": statistics.mean(ms), "gbs": by / (sum(ms) / 1000.0) / 1e9,
-                         "samples_per_frame": statistics.mean(samples[(dt, k)] for k in range(len(cams)))}
+                         "samples_per_frame": statistics.mean(samples[(dt, k)] for k in range(len(cams))),
+                         "compulsory_bytes_per_frame": compulsory,
+                         "compulsory_gbs": compulsory / (statistics.mean(ms) / 1000.0) / 1e9}
     for r in rend.values():
         r.close()
+    cpu = None
+    if not args.skip_cpu:
+        # the oracle on all host cores, one frame of camera 0 per storage
+        import oracle
+        from pyvr_gb300 import workloads as W
+        from pyvr_gb300.renderer import rgba_lut
+        oracle.build()
+        cpu = {"cores": oracle.max_threads(), "kind": "port", "per_storage": {}}
+        for dt, c in scenes.items():
+            s = W.frame_inputs(c["volume"], cams[0], c["light"], c["config"], rgba_lut(c["ctf"], c["otf"]),
+                               res, res, c["value_scale"])
+            t = time.perf_counter()
+            _, _, n = oracle.render(s, want_float=False)
+            dt_s = time.perf_counter() - t
+            cpu["per_storage"][dt] = {"ms_per_frame": 1000.0 * dt_s, "samples_per_s": n / dt_s,
+                                      "gpu_speedup": dt_s / (per_dtype[dt]["avg_launch_ms"] / 1000.0)}
+        cpu["sample"] = "one frame (camera 0) per storage"
     return {"frames_per_s": frames / elapsed, "e2e_frames_per_s": e2e,
             "ms_per_frame": 1000.0 * elapsed / frames,
             "samples_per_s": sum(samples[(dt, k)] for dt, k, _ in launch_ms) / elapsed,
@@ -722,7 +800,7 @@ def plain_section(args, torch):
                                      else None),
                          "traffic_note": "f32 frame, one full-size ncu launch",
                          "kernel": "march_single_kernel", "per_storage": per_dtype},
-            "gpu_launches": len(launch_ms),
+            "gpu_launches": len(launch_ms), "cpu_baseline": cpu, "c1": c1_section(args, torch),
             "config": {"volume": f"{n_vol}^3 value noise seed 0", "storages": list(rend),
                        "cameras": len(cams), "resolution": f"{res}x{res}", "render_config": args.plain_config,
                        "frames_per_step": len(rend) * len(cams),
