@@ -303,9 +303,9 @@ int pvr_render(pvr_renderer *r, uint8_t *out_rgba8, float *out_rgba32f) {
 }
 
 int pvr_render_pinned(pvr_renderer *r, const uint8_t **rgba8) {
-    if (int rc = check_handle(r)) return rc;
     if (!rgba8) return fail(PVR_ERR_VALUE, "rgba8 is NULL");
     *rgba8 = nullptr;
+    if (int rc = check_handle(r)) return rc;
     DeviceScope ds(r->device);
     const size_t npx = (size_t)r->width * r->height;
     if (!r->h_out8) PVR_CUDA(cudaMallocHost((void **)&r->h_out8, npx * 4));

@@ -79,6 +79,18 @@ def test_argument_checks_before_any_device_work(native_lib):
     assert lib.pvr_batch_render_static(None, 1, None, None) == E
     assert lib.pvr_batch_render_static(None, -1, None, None) == E
     assert lib.pvr_batch_render(None, None, 0, None) == E
+    cfg = _native.PvrServerConfig(8, 3, 0, 0, 0, _native.PvrTuning(0, 0, 0, 0), -1)
+    assert lib.pvr_server_create(ctypes.byref(cfg), ctypes.byref(out)) == E  # negative pixel budget
+    assert b"batch_pixels" in lib.pvr_last_error()
+    img = ctypes.c_void_p(1)
+    assert lib.pvr_render_pinned(None, ctypes.byref(img)) == E and not img.value
+    nbytes = ctypes.c_int(0)
+    assert lib.pvr_volume_record_bytes(None, ctypes.byref(nbytes)) == E
+
+
+def test_compact_records_switch(native_lib):
+    assert native_lib.pvr_set_compact_records(1) == _native.PVR_OK
+    assert native_lib.pvr_set_compact_records(0) == _native.PVR_OK  # back to the default
 
 
 def test_error_code_mapping():
