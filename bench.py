@@ -233,7 +233,7 @@ def serving_section(args, torch):
     its own resident copies of the same volumes, closed before the other arm
     starts, over the same request streams."""
     from pyvr_gb300 import workloads as W
-    from pyvr_gb300.replicas import barrier
+    from pyvr_gb300.replicas import all_ok, barrier
     from pyvr_gb300.server import NativeRenderServer, drive, latency_stats, sustained_rate
     t_setup = time.perf_counter()
     wl = W.ServingWorkload(n_volumes=args.serving_volumes, n_extra=args.serving_extra, min_dim=128,
@@ -264,7 +264,8 @@ def serving_section(args, torch):
             attempts.append({"offered": rate, "completed_per_s": len(reqs) / el, "p99_ms": lat.get("p99_ms"),
                              "lut_builds": impl.luts.misses - m0,
                              "uploaded_bytes": impl.cache.uploaded_bytes - up0})
-            if lat.get("p99_ms", 1e9) <= P99_MS:
+            # the ranks repeat together, so that their barriers stay paired
+            if all_ok(lat.get("p99_ms", 1e9) <= P99_MS, device="cuda"):
                 break
             rate *= 0.9
         return reqs, el, impl.stats(), attempts

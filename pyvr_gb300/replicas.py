@@ -1,7 +1,8 @@
 """Replicas across GPUs: one independent server or renderer per process and
 GPU, with no exchange on the data path (rays and requests are independent).
-The only collectives are the timing barrier around a measured region and the
-final aggregation of what every rank did."""
+The only collectives are the timing barrier around a measured region, the
+ranks' joint decision to repeat a measurement, and the final aggregation of
+what every rank did."""
 
 from __future__ import annotations
 
@@ -16,6 +17,19 @@ def barrier() -> None:
     d = _dist()
     if d is not None:
         d.barrier()
+
+
+def all_ok(flag: bool, device=None) -> bool:
+    """True on every rank if the flag is true on every rank: a decision the
+    ranks take together (e.g. whether a timed run is repeated), so that their
+    collectives stay paired.  With one process, the flag itself."""
+    d = _dist()
+    if d is None:
+        return bool(flag)
+    import torch
+    t = torch.tensor([1 if flag else 0], dtype=torch.int32, device=device)
+    d.all_reduce(t, op=d.ReduceOp.MIN)
+    return bool(t.item())
 
 
 def job_rate(count: float, elapsed_s: float, device=None) -> float:

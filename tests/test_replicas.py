@@ -30,6 +30,24 @@ def _worker(rank, world, port, counts, times, out):
         dist.destroy_process_group()
 
 
+def _vote_worker(rank, world, port, flags, out):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        from pyvr_gb300.replicas import all_ok
+        out[rank] = (all_ok(flags[rank]), all_ok(True))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_ranks_decide_together():
+    ctx = mp.get_context("spawn")
+    out = ctx.Manager().dict()
+    mp.start_processes(_vote_worker, args=(2, _free_port(), [True, False], out), nprocs=2,
+                       start_method="spawn")
+    assert out[0] == (False, True) and out[1] == (False, True)
+
+
 def test_job_rate_over_two_ranks():
     ctx = mp.get_context("spawn")
     out = ctx.Manager().dict()
