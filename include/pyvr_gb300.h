@@ -180,6 +180,10 @@ int pvr_volume_device_bytes(const pvr_volume *v, long long *bytes);
  * precision, as numpy does for float16 input).  No reference counterpart:
  * the GL path keeps voxels and normals in two textures (manager.py:77-135). */
 int pvr_volume_record_bytes(const pvr_volume *v, int *bytes);
+/* This volume's records as halves, if every one of their floats is a half
+ * exactly; *compacted (may be NULL) = 1 if the records are halves afterwards.
+ * No render may read the volume during the call.  No reference counterpart. */
+int pvr_volume_compact(pvr_volume *v, int *compacted);
 /* Whether layouts built after the call may use 8-byte records (default 0:
  * off).  Either form renders the same images; half records halve the
  * records' memory, cost decode instructions per sample, and pay only where

@@ -29,11 +29,12 @@ class DeviceVolume:
 
     normals: "given" (use ``volume.normals``), "device" (compute with
     numpy.gradient semantics on the GPU), "none", or "auto" (given if the
-    volume has normals, else none).
+    volume has normals, else none).  half_records: store the records as
+    halves if every value and normal is a half exactly (``compact``).
     """
 
     def __init__(self, volume, value_scale: float = 1.0, normals: str = "auto",
-                 brick_log2: int = 0):
+                 brick_log2: int = 0, half_records: bool = False):
         data, code = volume_storage(np.asarray(volume.data))
         mode = normals
         if mode == "auto":
@@ -63,6 +64,16 @@ class DeviceVolume:
         self.dtype = data.dtype
         self.normals_mode = mode
         self.brick_log2 = brick_log2 or 3
+        if half_records:
+            self.compact()
+
+    def compact(self) -> bool:
+        """Records as halves if every one of their floats is a half exactly
+        (the images stay the same); True if they are halves afterwards.  No
+        render may read the volume meanwhile."""
+        c = ctypes.c_int(0)
+        check(_lib().pvr_volume_compact(self.handle, ctypes.byref(c)))
+        return bool(c.value)
 
     def device_bytes(self) -> int:
         n = ctypes.c_longlong(0)

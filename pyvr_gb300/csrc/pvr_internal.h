@@ -147,6 +147,7 @@ namespace pvr {
 int fail(int code, const char *fmt, ...);
 int cuda_fail(cudaError_t e, const char *what);
 int ensure_volume_layout(pvr_volume *v, cudaStream_t st);
+int try_compact_records(pvr_volume *v, cudaStream_t st);
 cudaError_t vol_alloc(void **p, size_t bytes, cudaStream_t st);
 void vol_free(void *p, cudaStream_t st);
 void free_volume_buffers(pvr_volume *v, cudaStream_t st);

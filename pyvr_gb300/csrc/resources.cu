@@ -141,15 +141,26 @@ int ensure_volume_layout(pvr_volume *v, cudaStream_t st) {
                                   v->d_table, (float4 *)v->d_records, v->d_bricks, st));
     vol_free(v->d_nrm, st);  // given normals now live in the records
     v->d_nrm = nullptr;
-    // Half records when every value and normal is a half exactly: float16
-    // volumes with normals computed in half precision (numpy's arithmetic
-    // for float16 input) always are, uint8 values are too.  The march reads
-    // half as many bytes per sample and decodes the same floats.
+    v->compact = false;
+    PVR_CUDA(cudaStreamSynchronize(st));  // `table` leaves scope; ready for any stream
+    v->layout_ready = true;
+    if (g_compact_records.load()) try_compact_records(v, st);
+    return PVR_OK;
+}
+
+// Half records when every value and normal is a half exactly: float16
+// volumes with normals computed in half precision (numpy's arithmetic for
+// float16 input) always are, uint8 values are too.  The march reads half as
+// many bytes per sample and decodes the same floats.  The float records stay
+// when some float is not a half, or when the memory for the copy is missing.
+// Nothing may read the volume meanwhile.  Returns 1 if the records are halves.
+int try_compact_records(pvr_volume *v, cudaStream_t st) {
+    if (v->compact) return 1;
+    const size_t nrec = v->records_bytes / sizeof(float4);
     uint2 *compact = nullptr;
     int *d_flag = nullptr;
     int inexact = 1;
-    v->compact = false;
-    if (g_compact_records.load() && vol_alloc((void **)&compact, nrec * sizeof(uint2), st) == cudaSuccess) {
+    if (vol_alloc((void **)&compact, nrec * sizeof(uint2), st) == cudaSuccess) {
         if (vol_alloc((void **)&d_flag, sizeof(int), st) == cudaSuccess &&
             cudaMemsetAsync(d_flag, 0, sizeof(int), st) == cudaSuccess &&
             launch_compact_records((const float4 *)v->d_records, compact, (long long)nrec, d_flag, st) ==
@@ -157,7 +168,7 @@ int ensure_volume_layout(pvr_volume *v, cudaStream_t st) {
             cudaMemcpyAsync(&inexact, d_flag, sizeof(int), cudaMemcpyDeviceToHost, st);
     }
     cudaGetLastError();  // a failed allocation or launch above only means: keep the float records
-    PVR_CUDA(cudaStreamSynchronize(st));  // `table` leaves scope; ready for any stream
+    cudaStreamSynchronize(st);
     vol_free(d_flag, st);
     if (compact && inexact == 0) {
         vol_free(v->d_records, st);
@@ -167,9 +178,8 @@ int ensure_volume_layout(pvr_volume *v, cudaStream_t st) {
     } else {
         vol_free(compact, st);
     }
-    PVR_CUDA(cudaStreamSynchronize(st));
-    v->layout_ready = true;
-    return PVR_OK;
+    cudaStreamSynchronize(st);
+    return v->compact ? 1 : 0;
 }
 
 // Validated job -> the descriptor the kernel reads (everything the fragment
@@ -323,6 +333,25 @@ int pvr_volume_release(pvr_volume *v, void *stream) {
 
 int pvr_set_compact_records(int enabled) {
     pvr::g_compact_records.store(enabled ? 1 : 0);
+    return PVR_OK;
+}
+
+int pvr_volume_compact(pvr_volume *v, int *compacted) {
+    if (!v) return fail(PVR_ERR_VALUE, "NULL argument");
+    if (!v->layout_ready) return fail(PVR_ERR_STATE, "volume layout not built");
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev != v->device) cudaSetDevice(v->device);
+    cudaStream_t st = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        if (dev != v->device) cudaSetDevice(dev);
+        return pvr::cuda_fail(e, "cudaStreamCreateWithFlags");
+    }
+    const int c = pvr::try_compact_records(v, st);
+    cudaStreamDestroy(st);
+    if (dev != v->device) cudaSetDevice(dev);
+    if (compacted) *compacted = c;
     return PVR_OK;
 }
 

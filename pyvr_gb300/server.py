@@ -74,9 +74,10 @@ class RenderRequest:
 class VolumeCache:
     """HBM-resident volumes with a byte budget and LRU eviction."""
 
-    def __init__(self, budget_bytes: int, brick_log2: int = 3):
+    def __init__(self, budget_bytes: int, brick_log2: int = 3, half_records: bool = False):
         self.budget = int(budget_bytes)
         self.brick_log2 = brick_log2
+        self.half_records = half_records
         self._vols: "collections.OrderedDict[int, DeviceVolume]" = collections.OrderedDict()
         self._bytes: Dict[int, int] = {}
         self._users: Dict[int, int] = collections.defaultdict(int)  # in-flight batches
@@ -144,7 +145,7 @@ class VolumeCache:
             self._evict_for(est, release_after)
         normals = "given" if getattr(volume, "normals", None) is not None else "device"
         dv = DeviceVolume(volume, value_scale=value_scale, normals=normals,
-                          brick_log2=self.brick_log2)
+                          brick_log2=self.brick_log2, half_records=self.half_records)
         with self._lock:
             if vid in self._vols:  # loaded meanwhile by another request
                 release_after(dv)
@@ -619,15 +620,18 @@ class NativeRenderServer:
     defaults (8 slots, 512^2 pixels per launch) measured best on a mixed
     512^2 / 1024^2 stream.  ``lut_reserve`` tables of 256 entries are
     allocated at start, so that new transfer functions are built into
-    existing memory.  close() frees the resident volumes and tables."""
+    existing memory.  half_records: resident volumes whose values and normals
+    are all halves exactly (float16 volumes with device normals) keep their
+    records as halves: half the memory, the same images.  close() frees the
+    resident volumes and tables."""
 
     def __init__(self, budget_bytes: int = 40 << 30, max_batch: int = 64, slots: int = 8,
                  tuning: Optional[Tuning] = None, brick_log2: int = 3, loaders: int = 2,
                  instrument: int = 0, per_frame: bool = False, linger_us: int = 0,
-                 batch_pixels: int = 512 * 512, lut_reserve: int = 1024):
+                 batch_pixels: int = 512 * 512, lut_reserve: int = 1024, half_records: bool = False):
         import torch
         self.torch = torch
-        self.cache = VolumeCache(budget_bytes, brick_log2)
+        self.cache = VolumeCache(budget_bytes, brick_log2, half_records)
         self.luts = LutCache()
         self.luts.reserve(256, lut_reserve)
         self.per_frame = per_frame

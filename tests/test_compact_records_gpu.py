@@ -60,6 +60,33 @@ def test_float_records_by_default():
     assert DeviceVolume(Volume(data=data), normals="device").record_bytes() == 16
 
 
+def test_per_volume_half_records():
+    """DeviceVolume(half_records=True) compacts that volume alone, when exact."""
+    from pyvr_gb300 import Camera, Light, OpacityTransferFunction, RenderConfig
+    from pyvr_gb300.batch import BatchRenderer, DeviceLUT, RenderJob
+    base = W.value_noise((20, 18, 22), seed=5)
+    f16 = Volume(data=W.to_storage(base, "f16"), min_bounds=np.full(3, -1.0, np.float32),
+                 max_bounds=np.full(3, 1.0, np.float32))
+    half = DeviceVolume(f16, normals="device", half_records=True)
+    full = DeviceVolume(f16, normals="device")
+    assert half.record_bytes() == 8 and full.record_bytes() == 16
+    u8 = DeviceVolume(Volume(data=W.to_storage(base, "u8")), normals="device")
+    assert u8.compact() is False and u8.record_bytes() == 16
+    lut = DeviceLUT(W.standin_colormap(4), OpacityTransferFunction.linear(0.0, 0.4))
+    cam = Camera.from_spherical(np.zeros(3, np.float32), 0.4, 0.3, 0.0, 3.0)
+    outs = []
+    br = BatchRenderer(capacity=2, slots=2)
+    for dv in (half, full):
+        o8 = torch.zeros(64 * 48 * 4, dtype=torch.uint8, device="cuda")
+        of = torch.zeros(64 * 48 * 4, dtype=torch.float32, device="cuda")
+        br.render([RenderJob(dv, lut, cam, Light.default(), RenderConfig.balanced(), 64, 48, o8, of)])
+        br.synchronize()
+        outs.append((o8.cpu().numpy(), of.cpu().numpy()))
+    br.close()
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+    assert outs[0][0].reshape(-1, 4)[:, 3].max() > 0
+
+
 @pytest.mark.parametrize("n_jobs", [1, 9])
 def test_half_records_render_the_same_images(n_jobs):
     scenes = _mixed_scenes(n_jobs if n_jobs > 1 else 3, seed=31)

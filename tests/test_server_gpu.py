@@ -70,14 +70,15 @@ def test_server_with_evictions():
     assert stats["evictions"] > 0
 
 
-def _run_native(budget, n_req=160, per_frame=False, max_batch=16, slots=3, batch_pixels=0):
+def _run_native(budget, n_req=160, per_frame=False, max_batch=16, slots=3, batch_pixels=0,
+                half_records=False):
     """Results of the native server (batched or per-frame) and of the serial
     Python renderer for the same stream."""
     from pyvr_gb300.server import NativeRenderServer
     wl = _workload()
     stream = wl.requests(rate=4000.0, duration=1.0, seed=3)[:n_req]
     server = NativeRenderServer(budget_bytes=budget, max_batch=max_batch, slots=slots, per_frame=per_frame,
-                                instrument=1, batch_pixels=batch_pixels)
+                                instrument=1, batch_pixels=batch_pixels, half_records=half_records)
     serial = SerialRenderer()
     for slot in range(wl.n_catalog):
         vol, vs = wl.volumes[slot]
@@ -137,6 +138,14 @@ def test_native_server_concurrent_launches_complete_out_of_order():
     server.close()
     assert all(s.launched_at >= long.launched_at for s in short)
     assert any(s.done_at < long.done_at for s in short), [(s.launched_at, s.done_at) for s in short]
+
+
+def test_native_server_half_records_same_results():
+    # float16 volumes (device normals) held as half records: the same bytes as
+    # the float records of the per-request renderer
+    wl, stream, got, want, stats = _run_native(budget=40 << 30, max_batch=8, half_records=True)
+    for g, w in zip(got, want):
+        assert g.tobytes() == w
 
 
 def test_native_server_pixel_budget_per_launch():

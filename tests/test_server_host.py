@@ -16,7 +16,7 @@ from pyvr_gb300 import workloads as W
 class FakeDeviceVolume:
     made = []
 
-    def __init__(self, volume, value_scale=1.0, normals="auto", brick_log2=0):
+    def __init__(self, volume, value_scale=1.0, normals="auto", brick_log2=0, half_records=False):
         self.shape = volume.data.shape
         d, h, w = volume.data.shape
         lb = brick_log2 or 3  # the cache's own estimate of records + voxels
