@@ -820,7 +820,8 @@ def serving_config(args):
                          f"then {args.refine} bisection probes)",
             "server": (f"continuous batching over {args.slots} launch slots (streams), "
                        f"up to {args.max_batch} requests and {args.batch_pixels} pixels per launch, "
-                       f"linger {args.linger_us} us; "
+                       f"linger {args.linger_us} us, "
+                       f"{'half records where exact' if args.half_records else 'float records'}; "
                        "per-frame baseline: same runtime, one request per launch, each read back "
                        "before the next"),
             "parallelism": f"replicas x{args.gpus}",
