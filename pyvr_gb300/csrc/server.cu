@@ -5,10 +5,11 @@
 //  * submitters (any host thread): pvr_server_submit validates a request and
 //    appends it to the queue;
 //  * the scheduler: whenever a launch slot is free and requests are queued,
-//    takes up to max_batch of them (requests that arrived while other
-//    batches were on the GPU join the next batch), computes their camera
-//    matrices, and queues [batch march -> one copy of the slot's image arena
-//    to pinned host memory -> event] on the slot's stream;
+//    takes up to max_batch of them, and with batch_pixels > 0 only while
+//    their pixels sum to at most batch_pixels (requests that arrived while
+//    others were on the GPU join the next launch), and queues [march ->
+//    each image to its pinned destination (or the slot's pinned arena) ->
+//    event -> completion callback] on the slot's stream;
 //  * the completer: takes the slots whose work has finished, in the order
 //    they finish (a stream callback behind each slot's read-back hands the
 //    slot over and stamps the completion time), copies each image to its
