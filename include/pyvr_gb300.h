@@ -182,7 +182,9 @@ int pvr_volume_device_bytes(const pvr_volume *v, long long *bytes);
 int pvr_volume_record_bytes(const pvr_volume *v, int *bytes);
 /* This volume's records as halves, if every one of their floats is a half
  * exactly; *compacted (may be NULL) = 1 if the records are halves afterwards.
- * No render may read the volume during the call.  No reference counterpart. */
+ * The call first waits for all work queued on the volume's device (renders
+ * queued earlier may still read the records it replaces); no render of the
+ * volume may be queued while the call runs.  No reference counterpart. */
 int pvr_volume_compact(pvr_volume *v, int *compacted);
 /* Whether layouts built after the call may use 8-byte records (default 0:
  * off).  Either form renders the same images; half records halve the
@@ -264,8 +266,9 @@ int pvr_batch_synchronize(pvr_batch *b);
  * -- is a static 256-byte device array, so a call takes at most 6144 jobs
  * (PVR_ERR_VALUE beyond, nothing queued).  Calls whose work may overlap on a
  * device race on that array: keep them on one stream or order them.  The
- * first call on a device looks the array up (cudaGetSymbolAddress): make it
- * outside stream capture.  tuning: NULL for the default; stream: NULL for
+ * first call on a device looks the array up (cudaGetSymbolAddress), and so
+ * does the first call after the device's context was replaced
+ * (cudaDeviceReset): make those calls outside stream capture.  tuning: NULL for the default; stream: NULL for
  * the default stream. */
 int pvr_batch_render_static(const pvr_job *jobs, int n, const pvr_tuning *tuning, void *stream);
 

@@ -69,8 +69,9 @@ class DeviceVolume:
 
     def compact(self) -> bool:
         """Records as halves if every one of their floats is a half exactly
-        (the images stay the same); True if they are halves afterwards.  No
-        render may read the volume meanwhile."""
+        (the images stay the same); True if they are halves afterwards.  Waits
+        for all work queued on the volume's device first; no render of the
+        volume may be queued while it runs."""
         c = ctypes.c_int(0)
         check(_lib().pvr_volume_compact(self.handle, ctypes.byref(c)))
         return bool(c.value)

@@ -21,12 +21,14 @@
 //    may overlap on the GPU (different streams, or different host threads
 //    without ordering) race on them and can skip or repeat tiles.  Issue the
 //    calls on one stream, or order them with events;
-//  * the address of the static array is looked up once per device
-//    (cudaGetSymbolAddress, which also loads this module on that device);
-//    make the first call on each device outside stream capture.
+//  * the address of the static array is looked up once per device context
+//    (cudaGetSymbolAddress, which also loads this module on that device):
+//    on the first call on a device, and again on the first call after the
+//    device's context was replaced (cudaDeviceReset); make those calls
+//    outside stream capture.
 #include <algorithm>
-#include <atomic>
 #include <cstring>
+#include <mutex>
 #include <string>
 
 #include "pvr_internal.h"
@@ -38,18 +40,58 @@ constexpr int kMaxDevices = 64;
 
 __device__ __align__(256) static int g_tile_counters[kStaticCounters];
 
-std::atomic<int *> g_counter_addr[kMaxDevices];
+// The array's address in one device context: a context replaced by
+// cudaDeviceReset holds the module at a new address, so the cached address
+// is keyed by the context's process-unique id (cuCtxGetId).
+struct CounterAddr {
+    unsigned long long ctx_id;
+    int *ptr;
+};
+std::mutex g_counter_mutex;
+CounterAddr g_counter_addr[kMaxDevices];
+
+// cuCtxGetCurrent / cuCtxGetId from the driver the runtime already loaded
+// (no link-time dependency on libcuda).
+typedef int (*CtxGetCurrentFn)(void **);
+typedef int (*CtxGetIdFn)(void *, unsigned long long *);
+
+// Id of the calling thread's current context; 0 if none is current yet (the
+// runtime creates the primary context lazily) or if the driver entry points
+// are unavailable (then the address is cached per device alone).
+unsigned long long current_context_id() {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaDriverEntryPointQueryResult q;
+        void *f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<CtxGetIdFn>(f);
+    });
+    void *ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+    return id;
+}
 
 int counters_for_device(int device, int **out) {
     if (device < 0 || device >= kMaxDevices) return pvr::fail(PVR_ERR_VALUE, "device ordinal %d out of range", device);
-    int *p = g_counter_addr[device].load(std::memory_order_acquire);
-    if (!p) {
+    std::lock_guard<std::mutex> lock(g_counter_mutex);
+    CounterAddr &c = g_counter_addr[device];
+    const unsigned long long ctx = current_context_id();
+    if (!c.ptr || ctx == 0 || c.ctx_id != ctx) {
+        // also makes the device's primary context current if it was not yet
         void *addr = nullptr;
         PVR_CUDA(cudaGetSymbolAddress(&addr, g_tile_counters));
-        p = static_cast<int *>(addr);
-        g_counter_addr[device].store(p, std::memory_order_release);
+        c.ptr = static_cast<int *>(addr);
+        c.ctx_id = current_context_id();
     }
-    *out = p;
+    *out = c.ptr;
     return PVR_OK;
 }
 

@@ -80,17 +80,21 @@ void light_direction(const float pos[3], const float target[3], float out[3]) {
 // loading or evicting a volume does not stall renders running meanwhile.
 // The pool keeps freed memory for reuse instead of returning it at every
 // synchronisation.
+// The release threshold is set once per device (the first allocation on
+// each device), from any thread.
+constexpr int kMaxPoolDevices = 64;
+static std::atomic<bool> g_pool_configured[kMaxPoolDevices];
+
 cudaError_t vol_alloc(void **p, size_t bytes, cudaStream_t st) {
-    static bool pool_configured = false;
-    if (!pool_configured) {
-        int dev = 0;
-        cudaGetDevice(&dev);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev >= 0 && dev < kMaxPoolDevices && !g_pool_configured[dev].load(std::memory_order_acquire)) {
         cudaMemPool_t pool;
         if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
             uint64_t keep = UINT64_MAX;
             cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
         }
-        pool_configured = true;
+        g_pool_configured[dev].store(true, std::memory_order_release);
     }
     return cudaMallocAsync(p, bytes, st);
 }
@@ -342,8 +346,15 @@ int pvr_volume_compact(pvr_volume *v, int *compacted) {
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev != v->device) cudaSetDevice(v->device);
+    // Renders queued earlier on any stream may still read the float records
+    // that the swap frees: wait for all work on the volume's device first.
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        if (dev != v->device) cudaSetDevice(dev);
+        return pvr::cuda_fail(e, "cudaDeviceSynchronize");
+    }
     cudaStream_t st = nullptr;
-    cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         if (dev != v->device) cudaSetDevice(dev);
         return pvr::cuda_fail(e, "cudaStreamCreateWithFlags");

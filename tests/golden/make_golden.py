@@ -1,7 +1,7 @@
 """Generate golden host-side vectors by importing pyvr itself.
 
-Run in a checkout that has the reference tree (default /root/reference, or
-``--reference PATH``).  moderngl, matplotlib, PIL and vtk are replaced by
+Run with the reference tree at ``--reference PATH`` (default: the
+``PYVR_REFERENCE`` environment variable).  moderngl, matplotlib, PIL and vtk are replaced by
 empty import stubs: none of the functions sampled here touch them.
 
 Writes ``tests/golden/reference_host.npz`` holding, for a set of cases:
@@ -152,7 +152,10 @@ def main(reference: str, out: str) -> None:
 
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=os.environ.get("PYVR_REFERENCE"),
+                    help="path of the pyvr tree (default: $PYVR_REFERENCE)")
     ap.add_argument("--out", default=os.path.join(HERE, "reference_host.npz"))
     a = ap.parse_args()
+    if not a.reference:
+        ap.error("give --reference or set PYVR_REFERENCE")
     main(a.reference, a.out)

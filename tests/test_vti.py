@@ -12,7 +12,10 @@ import pytest
 from pyvr_gb300 import compute_normal_volume
 from pyvr_gb300.vti import load_vtk_volume, read_vti, write_vti
 
-EXAMPLES = os.path.join("/root/reference", "example_data")
+# the reference checkout, if present: PYVR_REFERENCE=<path to the pyvr tree>
+# (the tests that read its example files skip without it)
+_REFERENCE = os.environ.get("PYVR_REFERENCE")
+EXAMPLES = os.path.join(_REFERENCE, "example_data") if _REFERENCE else ""
 
 
 @pytest.mark.parametrize("fmt,encoding", [("ascii", "raw"), ("binary", "raw"), ("appended", "raw"),
@@ -80,7 +83,8 @@ def test_constant_volume_and_errors(tmp_path):
         load_vtk_volume(p2)
 
 
-@pytest.mark.skipif(not os.path.isdir(EXAMPLES), reason="reference example data not present")
+@pytest.mark.skipif(not (EXAMPLES and os.path.isdir(EXAMPLES)),
+                    reason="reference example data not present (set PYVR_REFERENCE)")
 @pytest.mark.parametrize("name,shape", [("hydrogen", (128, 128, 128)), ("fuel", (64, 64, 64))])
 def test_reference_example_files(name, shape):
     v = load_vtk_volume(Path(EXAMPLES) / f"{name}.vti")

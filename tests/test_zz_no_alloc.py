@@ -1,9 +1,14 @@
 """pvr_batch_render_static (the batch march that allocates nothing, scratch in
 a static device array) against pvr_batch_render on the same jobs: identical
-bytes, samples and counters, on two calls in a row.  Kept in its own file,
-collected last, so that it also runs after every other GPU test."""
+bytes, samples and counters, on two calls in a row; calls of different sizes
+queued back to back on one stream; and a warmed call that leaves the device's
+free memory, the default memory pool and torch's allocator untouched.  Kept
+in its own file, collected last, so that it also runs after every other GPU
+test."""
 
 import ctypes
+import gc
+import os
 
 import numpy as np
 import pytest
@@ -116,3 +121,87 @@ def test_static_batch_rejects_bad_calls():
     with pytest.raises(ValueError, match="without volume or LUT"):
         render_static(bad, 1)
     torch.cuda.synchronize()
+
+
+def test_static_batch_calls_of_different_sizes_back_to_back():
+    # a 200-job call (3 launches) and a 7-job call queued on one stream with
+    # no synchronisation between them: the second call's clear of the static
+    # counters runs behind every launch of the first
+    big, small = _scenes(200, seed=5), _scenes(7, seed=6)
+    sb, ss = _Setup(big, calls=2), _Setup(small, calls=2)
+    stream = torch.cuda.Stream()
+    br = BatchRenderer(capacity=200, slots=1)
+    br.render_structs(sb.structs(0), 200, stream=stream)
+    br.render_structs(ss.structs(0), 7, stream=stream)
+    stream.synchronize()
+    br.close()
+    render_static(sb.structs(1), 200, stream=stream)
+    render_static(ss.structs(1), 7, stream=stream)
+    stream.synchronize()
+    for setup in (sb, ss):
+        want, got = setup.results(0), setup.results(1)
+        for k, ((g8, gf, gc), (w8, wf, wc)) in enumerate(zip(got, want)):
+            assert np.array_equal(g8, w8), k
+            assert np.array_equal(gf.view(np.uint32), wf.view(np.uint32)), k
+            assert np.array_equal(gc, wc), k
+
+
+def _cudart():
+    """The CUDA runtime library torch loaded in this process (ctypes), or None."""
+    try:
+        with open("/proc/self/maps") as f:
+            paths = {line.split()[-1] for line in f if "libcudart.so" in line}
+    except OSError:
+        return None
+    for p in sorted(paths):
+        if os.path.exists(p):
+            try:
+                return ctypes.CDLL(p)
+            except OSError:
+                continue
+    return None
+
+
+def _pool_used_bytes(rt, device):
+    """Bytes in use from the device's default stream-ordered memory pool."""
+    pool = ctypes.c_void_p()
+    if rt.cudaDeviceGetDefaultMemPool(ctypes.byref(pool), device) != 0:
+        return None
+    used = ctypes.c_uint64()
+    if rt.cudaMemPoolGetAttribute(pool, 7, ctypes.byref(used)) != 0:  # cudaMemPoolAttrUsedMemCurrent
+        return None
+    return int(used.value)
+
+
+def test_static_batch_allocates_nothing():
+    setup = _Setup(_scenes(9, seed=7), calls=1)
+    structs = setup.structs(0)
+    stream = torch.cuda.Stream()
+    render_static(structs, 9, stream=stream)  # warm: module loaded, address looked up
+    stream.synchronize()
+    dev = torch.cuda.current_device()
+    rt = _cudart()
+    # objects of earlier tests freed meanwhile would change the free memory
+    gc.collect()
+    gc.disable()
+    try:
+        _measure_calls(structs, stream, dev, rt)
+    finally:
+        gc.enable()
+
+
+def _measure_calls(structs, stream, dev, rt):
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    pool0 = _pool_used_bytes(rt, dev) if rt is not None else None
+    stats0 = torch.cuda.memory_stats()
+    for _ in range(3):
+        render_static(structs, 9, stream=stream)
+    stream.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, "device memory changed across the calls"
+    if pool0 is not None:
+        assert _pool_used_bytes(rt, dev) == pool0, "the default memory pool grew"
+    stats1 = torch.cuda.memory_stats()
+    for k in ("allocation.all.allocated", "segment.all.allocated"):
+        assert stats1.get(k, 0) == stats0.get(k, 0), k
