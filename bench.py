@@ -42,6 +42,8 @@ import sys
 import tempfile
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -50,13 +52,17 @@ DTYPES = ("u8", "f16", "f32")
 RES = 1024
 N_VOL = 256
 NOMINAL_RATE = 400.0
-# DRAM bytes per in-box sample of the single-render march kernel on the
-# serving mix (ncu, 3 launches of a 4-volume serving case: 87.0 MB for about
-# 17.9 M samples) and DRAM bytes of one 1024^2 high_quality f32 frame of the
-# plain workload (ncu, one launch): the traffic estimates of the roofline
-# entries
-SERVING_DRAM_BYTES_PER_SAMPLE = 4.9
-PLAIN_F32_DRAM_BYTES_PER_FRAME = 100.4e6
+# Per shaded sample of the single-render march kernel (fast arithmetic, 16^3
+# bricks, half records) on a serving case whose catalog includes 512^3
+# volumes (ncu: smsp__inst_executed.sum and dram__bytes over the launches'
+# sample counters, profiles/march_single_kernel_serving_mix.md), and per
+# sample of the plain 256^3 high_quality frames
+# (profiles/march_single_kernel_256cube_1024px.md): the constants of the
+# roofline entries
+SERVING_WARP_INSTR_PER_SAMPLE = 9.4
+SERVING_DRAM_BYTES_PER_SAMPLE = 30.0
+PLAIN_WARP_INSTR_PER_SAMPLE = 9.0
+PLAIN_DRAM_BYTES_PER_SAMPLE = 1.2
 P99_MS = 20.0
 
 
@@ -78,10 +84,18 @@ def parse_args():
     ap.add_argument("--serving-brick-log2", type=int, default=4, help="brick size of the resident volumes")
     ap.add_argument("--serving-volumes", type=int, default=32)
     ap.add_argument("--serving-max-dim", type=int, default=512)
-    ap.add_argument("--serving-extra", type=int, default=16, help="volumes outside the catalog (loads)")
+    ap.add_argument("--serving-extra", type=int, default=224,
+                    help="volumes outside the catalog: the pool new-volume loads draw from (its records "
+                         "exceed the byte budget, so loads upload volumes that are not resident)")
+    ap.add_argument("--records", default="half_normals", choices=["float", "half_exact", "half_normals"],
+                    help="record form of the volumes laid out by the benchmark")
+    ap.add_argument("--arithmetic", default="fast", choices=["fast", "exact"],
+                    help="arithmetic of the march")
     # smaller cases for profiling captures
-    ap.add_argument("--only", choices=["all", "plain", "serving", "diff", "batching", "loaders"],
+    ap.add_argument("--only", choices=["all", "plain", "serving", "diff", "batching", "loaders", "requests"],
                     default="all")
+    ap.add_argument("--serving-min-dim", type=int, default=128)
+    ap.add_argument("--requests", type=int, default=24, help="requests section: renders of the stream")
     ap.add_argument("--loaders-volume", type=int, default=256, help="loaders section: volume extent")
     ap.add_argument("--diff-steps", type=int, default=200, help="Adam steps of the differentiation section")
     ap.add_argument("--no-tune", action="store_true", help="batching section: default tuning, no search")
@@ -92,8 +106,6 @@ def parse_args():
                     help="plain section: RenderConfig preset")
     ap.add_argument("--cameras", type=int, default=16)
     ap.add_argument("--skip-cpu", action="store_true")
-    ap.add_argument("--half-records", action="store_true",
-                    help="lay volumes out with 8-byte half records where they are exact")
     ap.add_argument("--skip-e2e", action="store_true")
     return ap.parse_args()
 
@@ -182,37 +194,90 @@ def gpu_index(local_rank):
 # CPU baseline: the oracle (a checker here, timed; never the product path)
 # ---------------------------------------------------------------------------
 
-def cpu_serving_sample(workload, target_s, seed, max_dim=256, max_req=400):
-    """Whole-frame oracle renders of render requests from the serving mix, in
-    arrival order, until target_s seconds of oracle time (at least one).
-    Catalog volumes up to max_dim^3 only, so that the host normals stay small.
-    Returns (seconds, requests, in-box samples, threads)."""
-    import oracle
-    from pyvr_gb300 import Volume, compute_normal_volume
-    from pyvr_gb300 import workloads as W
-    from pyvr_gb300.renderer import rgba_lut
-    oracle.build()
-    normals = {}  # id(data) -> (data, normals): the data reference keeps the id unique
-    total_t, total_n, done = 0.0, 0, 0
-    for _, kw in workload.requests(NOMINAL_RATE, 30.0, seed):
-        if kw["kind"] != "render" or kw["volume"].data.shape[0] > max_dim:
-            continue
-        v = kw["volume"]
-        if id(v.data) not in normals:
-            normals[id(v.data)] = (v.data, compute_normal_volume(v.data))
-        vol = Volume(data=v.data, normals=normals[id(v.data)][1], min_bounds=v.min_bounds,
-                     max_bounds=v.max_bounds)
-        lut = rgba_lut(kw["color_tf"], kw["opacity_tf"])
-        s = W.frame_inputs(vol, kw["camera"], kw["light"], kw["config"], lut, kw["width"], kw["height"],
-                           kw["value_scale"], batch_camera=True)
+class ReferenceServer:
+    """The reference's own host path serving the request mix, request by
+    request (no GPU, nothing of the pyvr_gb300 library): a new volume is
+    converted to float32 and gets its normals from ``compute_normal_volume``
+    (numpy, pyvr/datasets/synthetic.py:109-122) as the reference's
+    load_volume path does (pyvr/moderngl_renderer/renderer.py:107-146,
+    manager.py:88-97); the transfer functions become an RGBA table on the
+    host (manager.py:162-175); the camera matrices come from the ``Camera``
+    methods (pyvr/camera/camera.py:292-369); the frame is marched by the CPU
+    restatement of the shader (the oracle) on all host cores.  Volumes stay
+    resident (voxels + normals) under a host byte budget with LRU eviction."""
+
+    def __init__(self, budget_bytes=40 << 30):
+        import oracle
+        oracle.build()
+        self.oracle = oracle
+        self.budget = budget_bytes
+        self.resident = {}  # volume id -> (Volume, bytes), in LRU order
+
+    def _load(self, vid, vol):
+        from pyvr_gb300 import Volume, compute_normal_volume
+        self.resident.pop(vid, None)
+        data = vol.data.astype(np.float32)  # the reference uploads float32 textures
+        v = Volume(data=data, normals=compute_normal_volume(vol.data), min_bounds=vol.min_bounds,
+                   max_bounds=vol.max_bounds)
+        nbytes = data.nbytes + v.normals.nbytes
+        while self.resident and sum(b for _, b in self.resident.values()) + nbytes > self.budget:
+            self.resident.pop(next(iter(self.resident)))
+        self.resident[vid] = (v, nbytes)
+        return v
+
+    def make_resident(self, vid, vol):
+        """Untimed: the catalog volumes the stream starts with."""
+        if vid not in self.resident:
+            self._load(vid, vol)
+
+    def handle(self, kw):
+        """One request; returns (in-box samples, seconds of host work)."""
+        from pyvr_gb300 import workloads as W
+        from pyvr_gb300.renderer import rgba_lut
         t = time.perf_counter()
-        _, _, n = oracle.render(s, want_float=False)
-        total_t += time.perf_counter() - t
-        total_n += n
-        done += 1
-        if total_t >= target_s or done >= max_req:
-            break
-    return total_t, done, total_n, oracle.max_threads()
+        vid = kw["volume_id"]
+        if kw["kind"] == "load" or vid not in self.resident:
+            v = self._load(vid, kw["volume"])
+        else:
+            v = self.resident.pop(vid)[0]
+            self.resident[vid] = (v, v.data.nbytes + v.normals.nbytes)
+        lut = rgba_lut(kw["color_tf"], kw["opacity_tf"])
+        s = W.frame_inputs(v, kw["camera"], kw["light"], kw["config"], lut, kw["width"], kw["height"],
+                           kw["value_scale"])
+        _, _, n = self.oracle.render(s, want_float=False)
+        return n, time.perf_counter() - t
+
+
+def reference_serving_steps(wl, steps, seconds_per_step, seed, server=None):
+    """Request after request of the serving stream through ReferenceServer,
+    each step until `seconds_per_step` of host work; the catalog volumes a
+    request finds resident are made resident untimed.  Returns (per-step
+    [(requests, seconds, samples, loads)], threads)."""
+    server = server or ReferenceServer()
+    out = []
+
+    def requests():
+        k = 0
+        while True:  # 10-second chunks of the stream
+            for item in wl.requests(NOMINAL_RATE, 10.0, seed + 7919 * k):
+                yield item
+            k += 1
+
+    stream = requests()
+    for _ in range(steps):
+        nreq = ns = loads = 0
+        el = 0.0
+        while el < seconds_per_step:
+            _, kw = next(stream)
+            if kw["kind"] != "load":
+                server.make_resident(kw["volume_id"], kw["volume"])
+            n, dt = server.handle(kw)
+            nreq += 1
+            ns += n
+            el += dt
+            loads += kw["kind"] == "load"
+        out.append((nreq, el, ns, loads))
+    return out, server.oracle.max_threads()
 
 
 # ---------------------------------------------------------------------------
@@ -236,11 +301,18 @@ def serving_section(args, torch):
     from pyvr_gb300.replicas import all_ok, barrier
     from pyvr_gb300.server import NativeRenderServer, drive, latency_stats, sustained_rate
     t_setup = time.perf_counter()
-    wl = W.ServingWorkload(n_volumes=args.serving_volumes, n_extra=args.serving_extra, min_dim=128,
-                           max_dim=args.serving_max_dim, seed=0)
+    wl = W.ServingWorkload(n_volumes=args.serving_volumes, n_extra=args.serving_extra,
+                           min_dim=args.serving_min_dim, max_dim=args.serving_max_dim, seed=0)
+    wl.volumes.materialize()  # the clients' data exists before the stream starts
     pin_host_volumes(wl, torch)
     start = wl.snapshot()
     setup_s = time.perf_counter() - t_setup
+    from pyvr_gb300.server import VolumeCache
+    est = VolumeCache(0, args.serving_brick_log2)
+    pool = {"volumes": len(wl.volumes), "catalog": wl.n_catalog,
+            "host_bytes": int(sum(v.data.nbytes for v, _ in wl.volumes)),
+            "device_bytes_estimate": int(sum(est.estimate_bytes(v) - v.data.nbytes for v, _ in wl.volumes)),
+            "budget_bytes": 40 << 30}
     clocks = ClockSampler(gpu_index(dist_env()[2]))
 
     def timed_run(impl, rate, seed, reset):
@@ -252,8 +324,9 @@ def serving_section(args, torch):
             torch.cuda.synchronize()
             barrier()
             impl.reset_stats()
-            m0 = impl.luts.misses
-            up0 = impl.cache.uploaded_bytes
+            c = impl.cache
+            m0, up0, ld0, ev0, ob0, ar0 = (impl.luts.misses, c.uploaded_bytes, c.loads, c.evictions,
+                                           c.over_budget, c.alloc_retries)
             reset()
             clocks.start()
             reqs, el = drive(impl, wl.requests(rate, float(args.steps), seed))
@@ -261,9 +334,15 @@ def serving_section(args, torch):
             clocks.pause()
             barrier()
             lat = latency_stats(reqs)
+            load_lat = latency_stats([r for r in reqs if r.tag == "load"])
             attempts.append({"offered": rate, "completed_per_s": len(reqs) / el, "p99_ms": lat.get("p99_ms"),
                              "lut_builds": impl.luts.misses - m0,
-                             "uploaded_bytes": impl.cache.uploaded_bytes - up0})
+                             "uploaded_bytes": c.uploaded_bytes - up0, "volume_loads": c.loads - ld0,
+                             "evictions": c.evictions - ev0, "over_budget": c.over_budget - ob0,
+                             "alloc_retries": c.alloc_retries - ar0,
+                             "load_requests": sum(r.tag == "load" for r in reqs),
+                             "load_p50_ms": load_lat.get("p50_ms"), "load_p99_ms": load_lat.get("p99_ms"),
+                             "resident_bytes": c.used})
             # the ranks repeat together, so that their barriers stay paired
             if all_ok(lat.get("p99_ms", 1e9) <= P99_MS, device="cuda"):
                 break
@@ -275,8 +354,9 @@ def serving_section(args, torch):
         the timed steps of one implementation."""
         wl.restore(start)
         for slot in range(wl.n_catalog):
-            vol, vs = wl.volumes[slot]
-            impl.cache.insert(slot, vol, vs, impl._free_volume)
+            vid = wl.catalog[slot]
+            vol, vs = wl.volumes[vid]
+            impl.cache.insert(vid, vol, vs, impl._free_volume)
         torch.cuda.synchronize()
         # warm-up: W untimed one-second segments at the nominal rate (the same
         # streams for both implementations)
@@ -319,9 +399,11 @@ def serving_section(args, torch):
     nom = {"server": srv["nominal"], "serial": ser["nominal"]}
     probes_server, probes_serial = srv["probes"], ser["probes"]
     # our kernels in the timed region: the server's marches (one launch per
-    # batch), the per-frame marches, LUT builds of new transfer functions
+    # batch), the per-frame marches, LUT builds of new transfer functions and
+    # the layout of every uploaded volume
     launches = (st["batches"] + ser["stats"]["batches"] + srv_attempts[-1]["lut_builds"]
-                + ser_attempts[-1]["lut_builds"])
+                + ser_attempts[-1]["lut_builds"] + srv_attempts[-1]["volume_loads"]
+                + ser_attempts[-1]["volume_loads"])
     r_server, r_serial = srv_attempts[-1]["offered"], ser_attempts[-1]["offered"]
     # roofline of the server's march over the timed steps: algorithmic bytes
     # of the shaded samples (measured on every 8th launch, scaled to all
@@ -349,20 +431,53 @@ def serving_section(args, torch):
                kernel_ms=k_ms, inbox_samples=st["inbox_samples"], shaded_samples=st["shaded_samples"],
                mean_inbox_per_request=st["inbox_samples"] / max(1, st["instrumented_jobs"]),
                summed_launch_time_over_wall=k_ms * st["batches"] / inst / 1000.0 / srv_el,
-               roofline={"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_kind": peak_kind,
-                         "traffic": SERVING_DRAM_BYTES_PER_SAMPLE * st["shaded_samples"] / inst,
-                         "traffic_note": "per launch, scaled from a reduced-catalog ncu capture by samples",
-                         "algorithmic_bytes_per_launch": alg_per_launch,
-                         "launches": st["batches"], "launches_instrumented": st["instrumented_batches"],
-                         "mean_launch_ms_overlapped": k_ms / inst,
-                         "kernel": ("march_single_kernel" if st["max_jobs"] <= 1
-                                    else "march_batch_kernel + march_single_kernel"),
-                         "note": "algorithmic bytes of all timed launches over the timed wall time "
-                                 "(idle gaps included: a lower bound); launches overlap on the device"},
-               clocks=clk, h2d=h2d / args.steps, d2h=d2h / args.steps, setup_s=setup_s,
+               roofline=march_roofline(st["shaded_samples"] / inst * st["batches"], srv_el, clk,
+                                       SERVING_WARP_INSTR_PER_SAMPLE, SERVING_DRAM_BYTES_PER_SAMPLE,
+                                       alg_per_launch * st["batches"], torch,
+                                       kernel=("march_single_kernel" if st["max_jobs"] <= 1
+                                               else "march_batch_kernel + march_single_kernel"),
+                                       launches=st["batches"], launches_instrumented=st["instrumented_batches"],
+                                       note="samples of all timed launches (counted on every 8th launch, "
+                                            "scaled) over the timed wall time, idle gaps included: a lower "
+                                            "bound; launches overlap on the device",
+                                       profile="profiles/march_single_kernel_serving_mix.md"),
+               clocks=clk, h2d=h2d / args.steps, d2h=d2h / args.steps, setup_s=setup_s, pool=pool,
                loads=srv["loads"], evictions=srv["evictions"],
                lut_hits=srv["lut_hits"], lut_misses=srv["lut_misses"], workload=wl)
+    return out
+
+
+def march_roofline(samples, seconds, clocks, warp_instr_per_sample, dram_bytes_per_sample, alg_bytes, torch,
+                   **extra):
+    """Roofline of the march kernels.  They are bound by instruction issue
+    (the working sets of cached volumes sit in L1/L2) or by memory latency
+    (large volumes), not by HBM bandwidth.  bound "issue": warp instructions
+    per shaded sample (ncu, smsp__inst_executed.sum over the kernel's sample
+    counters) x shaded samples per second, against 4 issue slots per SM per
+    cycle at the median SM clock sampled during the timed region.  Beside it:
+    the DRAM bytes the kernel moves (ncu dram__bytes per sample x samples/s)
+    as a fraction of the measured HBM bandwidth, and the algorithmic bytes
+    (8 voxel + 8 float32x3 normal texels per sample, cache hits included)."""
+    peak_hbm, peak_kind = measured_peaks()
+    props = torch.cuda.get_device_properties(torch.cuda.current_device())
+    sms = props.multi_processor_count
+    mhz = (clocks or {}).get("sm_mhz") or (clocks or {}).get("sm_max_mhz") or 2070.0
+    peak_issue = sms * 4 * mhz * 1e6 / 1e9  # G warp instructions / s
+    rate = samples / seconds if seconds > 0 else 0.0
+    issue = warp_instr_per_sample * rate / 1e9
+    dram = dram_bytes_per_sample * rate / 1e9
+    out = {"bound": "issue", "achieved": issue, "peak": peak_issue, "unit": "G warp-instr/s",
+           "frac": issue / peak_issue if peak_issue else None,
+           "traffic": dram_bytes_per_sample * samples / max(1, extra.get("launches") or 1),
+           "traffic_note": "DRAM bytes per launch: ncu bytes per shaded sample x samples per launch",
+           "samples_per_s": rate, "warp_instr_per_sample": warp_instr_per_sample,
+           "issue_peak_note": f"{sms} SMs x 4 schedulers x {mhz:.0f} MHz (median sampled SM clock)",
+           "dram": {"achieved": dram, "peak": peak_hbm, "unit": "GB/s", "frac": dram / peak_hbm,
+                    "bytes_per_sample": dram_bytes_per_sample, "peak_kind": peak_kind},
+           "algorithmic": {"achieved": alg_bytes / seconds / 1e9 if seconds > 0 else 0.0, "unit": "GB/s",
+                           "frac_of_hbm": (alg_bytes / seconds / 1e9 / peak_hbm) if seconds > 0 else 0.0,
+                           "note": "8 voxel + 8 float32x3 normal texels per sample, L1/L2 hits included"}}
+    out.update(extra)
     return out
 
 
@@ -433,15 +548,16 @@ def batching_section(args, torch):
     ms_frames = timed(best, per_frame=True)
     dtypes = [s["dtype"] for s in scenes]
     shaded_bytes = sum(int(c[1]) * BYTES_PER_SAMPLE[dt] for c, dt in zip(per, dtypes))
-    peak, peak_kind = measured_peaks()
-    achieved = shaded_bytes / (ms_best / 1000.0) / 1e9
     return {"renders_per_s": len(scenes) / (ms_best / 1000.0), "ms_per_batch": ms_best,
             "default_tuning_ms_per_batch": ms_default, "per_frame_launches_ms": ms_frames,
             "tuning": dataclasses.asdict(best), "tuning_search_s": tune_s, "candidates": len(results),
             "candidate_ms": sorted(round(ms, 3) for _, ms in results)[:5],
             "samples_inbox": int(per[:, 0].sum()), "samples_shaded": int(per[:, 1].sum()),
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_kind": peak_kind, "kernel": "march_batch_kernel"},
+            "roofline": march_roofline(int(per[:, 1].sum()), ms_best / 1000.0, None, PLAIN_WARP_INSTR_PER_SAMPLE,
+                                       SERVING_DRAM_BYTES_PER_SAMPLE, shaded_bytes, torch,
+                                       kernel="march_batch_kernel", launches=1,
+                                       note="one batch launch; per-sample constants of the single-render "
+                                            "kernel (the batch kernel marches the same way)"),
             "config": {"renders": len(scenes), "volumes": "32..384 per axis log-uniform, u8/f16/f32 value noise",
                        "resolutions": "128^2..1024^2", "render_config": "balanced", "steps": args.steps}}
 
@@ -635,6 +751,45 @@ def loaders_section(args, torch):
     return out
 
 
+def requests_section(args, torch):
+    """The render requests of the serving stream one after the other, each a
+    single-render launch on one stream with sample counters: per launch, the
+    request's kind, volume, resolution, in-box and shaded samples and its
+    CUDA-event time.  Launch k of the march kernel here is request k, which
+    is what a profiler capture of these launches is matched against."""
+    from pyvr_gb300 import workloads as W
+    from pyvr_gb300.batch import BatchRenderer, DeviceLUT, DeviceVolume, RenderJob
+    wl = W.ServingWorkload(n_volumes=args.serving_volumes, n_extra=args.serving_extra,
+                           min_dim=args.serving_min_dim, max_dim=args.serving_max_dim, seed=0)
+    kws = [kw for _, kw in wl.requests(NOMINAL_RATE, 5.0, 31) if kw["kind"] == "render"][:args.requests]
+    vols, luts = {}, {}
+    for kw in kws:
+        if kw["volume_id"] not in vols:
+            vols[kw["volume_id"]] = DeviceVolume(kw["volume"], value_scale=kw["value_scale"], normals="device",
+                                                 brick_log2=args.serving_brick_log2)
+    br = BatchRenderer(capacity=1, slots=2)
+    stream = torch.cuda.Stream()
+    out = []
+    for kw in kws:
+        lut = DeviceLUT(kw["color_tf"], kw["opacity_tf"])
+        o8 = torch.empty(kw["width"] * kw["height"] * 4, dtype=torch.uint8, device="cuda")
+        cnt = torch.zeros(2, dtype=torch.int64, device="cuda")
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        br.render([RenderJob(vols[kw["volume_id"]], lut, kw["camera"], kw["light"], kw["config"], kw["width"],
+                             kw["height"], o8, None, cnt)], stream=stream)
+        b.record(stream)
+        stream.synchronize()
+        v = kw["volume"].data
+        out.append({"tag": kw["tag"], "volume": list(v.shape), "storage": str(v.dtype), "res": kw["width"],
+                    "inbox": int(cnt[0]), "shaded": int(cnt[1]), "ms": a.elapsed_time(b)})
+        luts[len(out)] = lut
+    br.close()
+    return {"launches": out, "shaded": sum(r["shaded"] for r in out),
+            "config": {"catalog": f"{args.serving_volumes} volumes {args.serving_min_dim}..{args.serving_max_dim}",
+                       "records": args.records, "arithmetic": args.arithmetic}}
+
+
 def c1_section(args, torch):
     """The small plain case (64^3 float32 double sphere, 256^2, balanced):
     device-timed frames, frames through render(), and the oracle on all host
@@ -794,13 +949,13 @@ def plain_section(args, torch):
     return {"frames_per_s": frames / elapsed, "e2e_frames_per_s": e2e,
             "ms_per_frame": 1000.0 * elapsed / frames,
             "samples_per_s": sum(samples[(dt, k)] for dt, k, _ in launch_ms) / elapsed,
-            "roofline": {"bound": "hbm", "achieved": tot_bytes / tot_s / 1e9, "peak": peak, "unit": "GB/s",
-                         "frac": tot_bytes / tot_s / 1e9 / peak, "peak_kind": peak_kind,
-                         "traffic": (PLAIN_F32_DRAM_BYTES_PER_FRAME
-                                     if "f32" in rend and (n_vol, res, args.plain_config) == (N_VOL, RES, "high_quality")
-                                     else None),
-                         "traffic_note": "f32 frame, one full-size ncu launch",
-                         "kernel": "march_single_kernel", "per_storage": per_dtype},
+            "roofline": march_roofline(sum(shaded[(dt, k)] for dt, k, _ in launch_ms), tot_s, None,
+                                       PLAIN_WARP_INSTR_PER_SAMPLE, PLAIN_DRAM_BYTES_PER_SAMPLE, tot_bytes,
+                                       torch, kernel="march_single_kernel", launches=len(launch_ms),
+                                       per_storage=per_dtype,
+                                       note="shaded samples over the summed CUDA-event times of the launches "
+                                            "(one after the other on one stream); issue peak at the maximum "
+                                            "SM clock", profile="profiles/march_single_kernel_256cube_1024px.md"),
             "gpu_launches": len(launch_ms), "cpu_baseline": cpu, "c1": c1_section(args, torch),
             "config": {"volume": f"{n_vol}^3 value noise seed 0", "storages": list(rend),
                        "cameras": len(cams), "resolution": f"{res}x{res}", "render_config": args.plain_config,
@@ -820,21 +975,23 @@ def serving_config(args):
                          f"then {args.refine} bisection probes)",
             "server": (f"continuous batching over {args.slots} launch slots (streams), "
                        f"up to {args.max_batch} requests and {args.batch_pixels} pixels per launch, "
-                       f"linger {args.linger_us} us, "
-                       f"{'half records where exact' if args.half_records else 'float records'}; "
+                       f"linger {args.linger_us} us, {args.records} records, {args.arithmetic} arithmetic; "
                        "per-frame baseline: same runtime, one request per launch, each read back "
-                       "before the next"),
+                       "before the next, a new volume loaded before anything that arrives after it"),
+            "loads": (f"a pool of {args.serving_volumes + args.serving_extra} volumes whose records exceed the "
+                      "40 GB budget; a load brings the volume out of the catalog longest (not resident), "
+                      "uploads it from pinned host memory and lays it out with device normals; LRU evicts"),
             "parallelism": f"replicas x{args.gpus}",
-            "l2": "resident volumes (~25 GB) far exceed L2"}
+            "l2": "resident volumes (tens of GB) far exceed L2"}
 
 
 def run_ours(args):
     import torch
     rank, world, local_rank = dist_env()
     torch.cuda.set_device(local_rank)
-    if args.half_records:
-        from pyvr_gb300.batch import set_compact_records
-        set_compact_records(True)
+    from pyvr_gb300.batch import set_arithmetic, set_compact_records
+    set_compact_records(args.records)
+    set_arithmetic(args.arithmetic)
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
@@ -842,6 +999,10 @@ def run_ours(args):
     diff = diff_section(args, torch) if args.only in ("all", "diff") else None
     batching = batching_section(args, torch) if args.only in ("all", "batching") else None
     loaders = loaders_section(args, torch) if args.only in ("all", "loaders") else None
+    if args.only == "requests":
+        if rank == 0:
+            print(json.dumps({"requests": requests_section(args, torch)}))
+        return
     if args.only in ("plain", "diff", "batching", "loaders"):
         if rank == 0:
             print(json.dumps({"plain": plain, "differentiation": diff, "batching_c3": batching,
@@ -858,23 +1019,19 @@ def run_ours(args):
         serial_value = job_rate(n_ser, el_ser, device="cuda")
     cpu = None
     if rank == 0 and not args.skip_cpu:
-        ct, nreq, cn, threads = cpu_serving_sample(s["workload"], args.cpu_seconds, 700)
+        steps, threads = reference_serving_steps(s["workload"], 1, args.cpu_seconds, 700)
+        nreq, ct, cn, nl = steps[0]
         cpu = {"value": nreq / ct, "unit": "renders/s", "cores": threads, "kind": "port",
-               "sample": f"oracle, whole frames of the first {nreq} render requests of a stream of the "
-                         f"mix (catalog volumes <= 256^3) in {ct:.1f} s on {threads} threads",
+               "sample": f"the reference's host path (float32 conversion and numpy normals for loads, "
+                         f"Camera matrices, host LUTs) and the oracle on whole frames: the first {nreq} "
+                         f"requests of a stream of the mix ({nl} loads) in {ct:.1f} s on {threads} threads",
                "samples_per_s": cn / ct}
     if rank == 0:
         srv = s["server"]
-        line = {"metric": "renders/s (batched server, mixed request stream, p99 <= 20 ms)",
-                "value": value, "unit": "renders/s", "n_gpus": world, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": 1000.0,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-                "data": "synthetic", "config": serving_config(args),
-                "p50_ms": srv.get("p50_ms"), "p99_ms": srv.get("p99_ms"),
-                "serial_per_frame": {"renders_per_s": serial_value, "p50_ms": s["serial"].get("p50_ms"),
-                                     "p99_ms": s["serial"].get("p99_ms"), "sustained_offered": s["rate_serial"]},
-                "server_over_serial": value / serial_value if serial_value else None,
-                "sustained_offered": s["rate_server"],
+        att, satt = s["attempts"]["server"][-1], s["attempts"]["serial"][-1]
+        # nested sections first, the headline's own keys last: the end of
+        # the line is what a log tail keeps
+        line = {"plain": plain, "batching_c3": batching, "differentiation": diff, "loaders": loaders,
                 "nominal_400": s["nominal"],
                 "probes": {"server": s["probes_server"], "serial": s["probes_serial"]},
                 "timed_attempts": s["attempts"],
@@ -883,23 +1040,44 @@ def run_ours(args):
                              "summed_launch_time_over_wall": s["summed_launch_time_over_wall"],
                              "server": {"max_batch": args.max_batch, "slots": args.slots,
                                         "batch_pixels": args.batch_pixels, "linger_us": args.linger_us},
-                             "loads": s["loads"], "evictions": s["evictions"],
                              "lut_builds_timed": s["lut_builds"], "lut_hits": s["lut_hits"],
                              "lut_misses": s["lut_misses"]},
                 "samples": {"inbox": s["inbox_samples"], "shaded": s["shaded_samples"],
                             "mean_inbox_per_request": s["mean_inbox_per_request"]},
-                "roofline": s["roofline"], "cpu_baseline": cpu, "clocks": s["clocks"],
+                "pool": s["pool"], "roofline": s["roofline"], "cpu_baseline": cpu,
+                "metric": "renders/s (batched server, mixed request stream, p99 <= 20 ms)",
+                "value": value, "unit": "renders/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1000.0,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic", "config": serving_config(args), "clocks": s["clocks"],
                 "e2e": {"value": value, "unit": "renders/s", "h2d_bytes_per_step": s["h2d"],
                         "d2h_bytes_per_step": s["d2h"]},
                 "gpu_launches": s["launches"],
-                "plain": plain, "batching_c3": batching, "differentiation": diff, "loaders": loaders}
+                "serial_per_frame": {"renders_per_s": serial_value, "p50_ms": s["serial"].get("p50_ms"),
+                                     "p99_ms": s["serial"].get("p99_ms"), "sustained_offered": s["rate_serial"],
+                                     "volume_loads": satt["volume_loads"], "evictions": satt["evictions"]},
+                "timed_loads": {"load_requests": att["load_requests"], "volume_loads": att["volume_loads"],
+                                "uploaded_bytes": att["uploaded_bytes"], "evictions": att["evictions"],
+                                "over_budget": att["over_budget"], "alloc_retries": att["alloc_retries"],
+                                "load_p50_ms": att["load_p50_ms"], "load_p99_ms": att["load_p99_ms"]},
+                "roofline_issue_frac": s["roofline"]["frac"], "roofline_dram_frac": s["roofline"]["dram"]["frac"],
+                "sustained_offered": s["rate_server"], "p50_ms": srv.get("p50_ms"), "p99_ms": srv.get("p99_ms"),
+                "server_over_serial": value / serial_value if serial_value else None}
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
 
 
 def run_reference(args):
-    """The oracle (CPU, all host cores) serving the same request mix."""
+    """The reference's own host path (no GPU, nothing of the pyvr_gb300 CUDA
+    library): float32 conversion and numpy normals for new volumes, the
+    Camera methods' matrices, host LUTs, and the CPU restatement of the
+    shader (the oracle) on all host cores, serving the same request mix one
+    request after another.  Each step is a bounded sample of the stream (at
+    least --cpu-seconds / --steps seconds of host work, one second at least);
+    the value is requests over the timed host seconds.  Volume data is
+    generated (numpy) and the catalog volumes a request finds resident get
+    their normals outside the timed work."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
@@ -907,26 +1085,26 @@ def run_reference(args):
     wl = W.ServingWorkload(n_volumes=args.serving_volumes, n_extra=args.serving_extra, min_dim=128,
                            max_dim=args.serving_max_dim, seed=0,
                            generator=lambda n, s: W.value_noise((n, n, n), s))
-    times, reqs, samples = [], 0, 0
-    threads = 1
     per_step = max(1.0, args.cpu_seconds / max(1, args.steps))
-    for i in range(args.warmup + args.steps):
-        t, nreq, n, threads = cpu_serving_sample(wl, per_step if i >= args.warmup else 0.0, 800 + i)
-        if i >= args.warmup:
-            times.append(t)
-            reqs += nreq
-            samples += n
-    value = reqs / sum(times) if times else 0.0
+    server = ReferenceServer()
+    reference_serving_steps(wl, args.warmup, per_step, 800, server)
+    steps, threads = reference_serving_steps(wl, args.steps, per_step, 900, server)
+    reqs = sum(n for n, _, _, _ in steps)
+    secs = sum(t for _, t, _, _ in steps)
+    samples = sum(x for _, _, x, _ in steps)
+    loads = sum(l for _, _, _, l in steps)
+    value = reqs / secs if secs else 0.0
     line = {"impl": "reference", "metric": "renders/s (batched server, mixed request stream, p99 <= 20 ms)",
             "value": value, "unit": "renders/s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1000 * statistics.mean(times), "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": 1000 * secs / max(1, len(steps)), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": serving_config(args),
             "cpu_baseline": {"kind": "port", "cores": threads, "value": value, "unit": "renders/s",
-                             "sample": f"per step: whole frames of render requests of the mix (catalog "
-                                       f"volumes <= 256^3) for >= {per_step:.1f} s of oracle time on "
-                                       f"{threads} threads; {reqs} requests in {sum(times):.1f} s",
-                             "samples_per_s": samples / sum(times) if times else 0.0},
+                             "sample": f"per step: requests of the mix in stream order (catalog volumes "
+                                       f"128^3-512^3, 1024^2 captures, new-volume loads with numpy normals) "
+                                       f"for >= {per_step:.1f} s of host work on {threads} threads; "
+                                       f"{reqs} requests ({loads} loads) in {secs:.1f} s",
+                             "samples_per_s": samples / secs if secs else 0.0},
             "e2e": {"value": value, "unit": "renders/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 

@@ -156,9 +156,10 @@ int pvr_frame_constants(const float view[16], const float proj[16], const float 
  * shareable device objects so many renders run in one launch).
  * ------------------------------------------------------------------------ */
 
-/* A volume on the device: the (D,H,W) voxels of `data` in their own storage
- * type plus the bricked texel records the march reads (the volume and normal
- * textures of manager.py:77-135).  normals_mode: PVR_NORMALS_NONE (shade
+/* A volume on the device: the bricked texel records the march reads (the
+ * volume and normal textures of manager.py:77-135), laid out on the device
+ * from the (D,H,W) voxels of `data`, which are uploaded in their own storage
+ * type and released once the records (which hold every stored value) exist.  normals_mode: PVR_NORMALS_NONE (shade
  * with normalize(density,0,0)), PVR_NORMALS_GIVEN (`normals` = host float32
  * (D,H,W,3)), PVR_NORMALS_DEVICE (computed on the device with the semantics
  * of pyvr/datasets/synthetic.py:109-122 compute_normal_volume, in the
@@ -186,11 +187,35 @@ int pvr_volume_record_bytes(const pvr_volume *v, int *bytes);
  * queued earlier may still read the records it replaces); no render of the
  * volume may be queued while the call runs.  No reference counterpart. */
 int pvr_volume_compact(pvr_volume *v, int *compacted);
-/* Whether layouts built after the call may use 8-byte records (default 0:
- * off).  Either form renders the same images; half records halve the
- * records' memory, cost decode instructions per sample, and pay only where
- * the march waits on memory (large volumes). */
-int pvr_set_compact_records(int enabled);
+/* Which layouts built after the call use 8-byte half records {value, nx, ny,
+ * nz} instead of 16-byte float records (no reference counterpart; the GL
+ * path keeps voxels and normals in two textures, manager.py:77-135):
+ * PVR_RECORDS_FLOAT (0, the default): never; PVR_RECORDS_HALF_EXACT (1): when
+ * every value and normal component is a half exactly (the images are then
+ * identical); PVR_RECORDS_HALF_NORMALS (2): when every value is a half
+ * exactly (uint8 and float16 volumes keep their values), with the normal
+ * components rounded to half (relative error <= 2^-11 each).  Half records
+ * halve the records' memory and the bytes a sample reads, and cost two
+ * decode instructions per record. */
+enum pvr_records { PVR_RECORDS_FLOAT = 0, PVR_RECORDS_HALF_EXACT = 1, PVR_RECORDS_HALF_NORMALS = 2 };
+int pvr_set_compact_records(int mode);
+int pvr_get_compact_records(int *mode);
+/* *exact = 1 if the volume's records hold its values and normals exactly
+ * (float records, or half records of halves), 0 if normals were rounded. */
+int pvr_volume_records_exact(const pvr_volume *v, int *exact);
+
+/* Arithmetic of the march for renders queued after the call, on every
+ * entry point (no reference counterpart: GLSL leaves rounding to the
+ * driver).  PVR_ARITH_FAST (0, the default): the same samples of the same
+ * texels with the same lerps and LUT addressing as the exact arithmetic;
+ * the shading tail contracts products into FMAs and takes exp and 1/sqrt
+ * from one hardware instruction each, so images are within 1 LSB per RGBA8
+ * channel of the exact ones, not bit-identical.  PVR_ARITH_EXACT (1): every
+ * operation rounded as the CPU oracle rounds it, so images equal the
+ * oracle's bit for bit.  A call reads the setting once for all its jobs. */
+enum pvr_arithmetic { PVR_ARITH_FAST = 0, PVR_ARITH_EXACT = 1 };
+int pvr_set_arithmetic(int mode);
+int pvr_get_arithmetic(int *mode);
 /* The float32 (D,H,W,3) normals held in the records (host buffer): what
  * Volume.normals holds after compute_normal_volume (pyvr/volume/data.py:103-118),
  * read back from the device. */

@@ -107,6 +107,10 @@ SIGNATURES = {
     "pvr_render": (_I, [_VP, _VP, _VP]),
     "pvr_volume_record_bytes": (_I, [_VP, ctypes.POINTER(_I)]),
     "pvr_set_compact_records": (_I, [_I]),
+    "pvr_get_compact_records": (_I, [ctypes.POINTER(_I)]),
+    "pvr_volume_records_exact": (_I, [_VP, ctypes.POINTER(_I)]),
+    "pvr_set_arithmetic": (_I, [_I]),
+    "pvr_get_arithmetic": (_I, [ctypes.POINTER(_I)]),
     "pvr_volume_compact": (_I, [_VP, ctypes.POINTER(_I)]),
     "pvr_render_pinned": (_I, [_VP, ctypes.POINTER(_VP)]),
     "pvr_render_device": (_I, [_VP, _VP, _VP, _VP]),

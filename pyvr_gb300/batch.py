@@ -88,6 +88,13 @@ class DeviceVolume:
         check(_lib().pvr_volume_record_bytes(self.handle, ctypes.byref(n)))
         return int(n.value)
 
+    def records_exact(self) -> bool:
+        """True if the records hold the values and normals exactly (False:
+        half records with the normals rounded to half)."""
+        e = ctypes.c_int(0)
+        check(_lib().pvr_volume_records_exact(self.handle, ctypes.byref(e)))
+        return bool(e.value)
+
     def read_normals(self) -> np.ndarray:
         out = np.empty(self.shape + (3,), dtype=np.float32)
         check(_lib().pvr_volume_read_normals(self.handle, out.ctypes.data))
@@ -105,12 +112,62 @@ class DeviceVolume:
             pass
 
 
-def set_compact_records(enabled: bool) -> None:
-    """Allow or forbid (default) 8-byte half records for volumes laid out
-    from now on.  Either form renders the same images; half records halve
-    the records' memory of float16 volumes and pay in speed only where the
-    march waits on memory (large volumes)."""
-    check(_lib().pvr_set_compact_records(int(bool(enabled))))
+_RECORD_MODES = {"float": 0, "half_exact": 1, "half_normals": 2}
+
+
+def set_compact_records(mode) -> None:
+    """Record form of volumes laid out from now on: "float" (or False; 16-byte
+    float records), "half_exact" (or True; 8-byte half records where every
+    value and normal component is a half exactly: identical images) or
+    "half_normals" (half records for volumes whose values are halves exactly
+    -- uint8 and float16 -- with the normal components rounded to half)."""
+    if isinstance(mode, bool):
+        mode = "half_exact" if mode else "float"
+    if mode not in _RECORD_MODES:
+        raise ValueError(f"record mode must be one of {sorted(_RECORD_MODES)}, got {mode!r}")
+    check(_lib().pvr_set_compact_records(_RECORD_MODES[mode]))
+
+
+def get_compact_records() -> str:
+    m = ctypes.c_int(0)
+    check(_lib().pvr_get_compact_records(ctypes.byref(m)))
+    return {v: k for k, v in _RECORD_MODES.items()}[m.value]
+
+
+_ARITHMETIC = {"fast": 0, "exact": 1}
+
+
+def set_arithmetic(mode: str) -> None:
+    """Arithmetic of renders queued from now on, on every entry point:
+    "fast" (the default: FMA-contracted shading with hardware exp and
+    1/sqrt, within 1 LSB per RGBA8 channel of "exact") or "exact" (every
+    operation rounded as the CPU oracle rounds it: bit-identical images)."""
+    if mode not in _ARITHMETIC:
+        raise ValueError(f"arithmetic must be 'fast' or 'exact', got {mode!r}")
+    check(_lib().pvr_set_arithmetic(_ARITHMETIC[mode]))
+
+
+def get_arithmetic() -> str:
+    m = ctypes.c_int(0)
+    check(_lib().pvr_get_arithmetic(ctypes.byref(m)))
+    return {v: k for k, v in _ARITHMETIC.items()}[m.value]
+
+
+class arithmetic:
+    """Context manager: ``with arithmetic("exact"): ...`` renders with the
+    given arithmetic and restores the previous one on exit."""
+
+    def __init__(self, mode: str):
+        self.mode = mode
+
+    def __enter__(self):
+        self.prev = get_arithmetic()
+        set_arithmetic(self.mode)
+        return self
+
+    def __exit__(self, *exc):
+        set_arithmetic(self.prev)
+        return False
 
 
 class DeviceLUT:

@@ -17,21 +17,21 @@
 #include "pvr_internal.h"
 
 namespace pvr {
-const void *batch_kernel_b2(const Tuning &);
-const void *batch_kernel_b3(const Tuning &);
-const void *batch_kernel_b4(const Tuning &);
+const void *batch_kernel_b2(const Tuning &, int);
+const void *batch_kernel_b3(const Tuning &, int);
+const void *batch_kernel_b4(const Tuning &, int);
 const void *single_kernel_b2(const Tuning &, int);
 const void *single_kernel_b3(const Tuning &, int);
 const void *single_kernel_b4(const Tuning &, int);
-int max_batch_blocks_b2(const Tuning &, int);
-int max_batch_blocks_b3(const Tuning &, int);
-int max_batch_blocks_b4(const Tuning &, int);
+int max_batch_blocks_b2(const Tuning &, int, int);
+int max_batch_blocks_b3(const Tuning &, int, int);
+int max_batch_blocks_b4(const Tuning &, int, int);
 
-const void *batch_kernel(int log2b, const Tuning &t) {
+const void *batch_kernel(int log2b, const Tuning &t, int variant) {
     switch (log2b) {
-    case 2: return batch_kernel_b2(t);
-    case 4: return batch_kernel_b4(t);
-    default: return batch_kernel_b3(t);
+    case 2: return batch_kernel_b2(t, variant);
+    case 4: return batch_kernel_b4(t, variant);
+    default: return batch_kernel_b3(t, variant);
     }
 }
 
@@ -47,12 +47,18 @@ size_t batch_smem_bytes(int lut_smem_entries) {
     return (size_t)lut_smem_entries * sizeof(float4) + (size_t)(lut_smem_entries + 1) * sizeof(int);
 }
 
-int max_batch_blocks_per_sm(int log2b, const Tuning &t, int lut_smem_entries) {
+int max_batch_blocks_per_sm(int log2b, const Tuning &t, int lut_smem_entries, int variant) {
     switch (log2b) {
-    case 2: return max_batch_blocks_b2(t, lut_smem_entries);
-    case 4: return max_batch_blocks_b4(t, lut_smem_entries);
-    default: return max_batch_blocks_b3(t, lut_smem_entries);
+    case 2: return max_batch_blocks_b2(t, lut_smem_entries, variant);
+    case 4: return max_batch_blocks_b4(t, lut_smem_entries, variant);
+    default: return max_batch_blocks_b3(t, lut_smem_entries, variant);
     }
+}
+
+int job_variant_of(const pvr_job &j, bool fast) {
+    return (j.volume->normals_mode != PVR_NORMALS_NONE ? kSingleNormals : 0) |
+           (j.lut->size <= kMaxSmemLut ? kSingleSmemLut : 0) | (j.volume->compact ? kSingleCompact : 0) |
+           (fast ? kSingleFast : 0);
 }
 }  // namespace pvr
 
@@ -151,7 +157,11 @@ int build_graph(Slot &s, const LaunchKey &key, void **args) {
     return PVR_OK;
 }
 
-int launch_chunk(pvr_batch *b, const pvr_job *jobs, int n, cudaStream_t st) {
+// One launch over jobs[idx[0..n)] (jobs of one variant, at most
+// kMaxLaunchJobs).
+int launch_chunk(pvr_batch *b, const pvr_job *all, const int *idx, int n, bool fast, cudaStream_t st) {
+    std::vector<pvr_job> jobs(n);
+    for (int i = 0; i < n; ++i) jobs[i] = all[idx[i]];
     const int log2b = jobs[0].volume->log2b;
     int max_lut = 1;
     for (int i = 0; i < n; ++i) max_lut = std::max(max_lut, jobs[i].lut->size);
@@ -165,15 +175,15 @@ int launch_chunk(pvr_batch *b, const pvr_job *jobs, int n, cudaStream_t st) {
         // launched directly (its parameters are copied at the launch, and it
         // uses no work counter); the slot's event tracks it like a batch
         pvr::SingleParams &sp = b->single;
-        if (int rc = pvr::fill_job(jobs[0], b->tuning.tile_w, b->tuning.tile_h, sp.job)) return rc;
+        if (int rc = pvr::fill_job(jobs[0], b->tuning.tile_w, b->tuning.tile_h, fast, sp.job)) return rc;
         sp.tile_w = b->tuning.tile_w;
         sp.tile_h = b->tuning.tile_h;
         int lut_smem = 256;
-        while (lut_smem < max_lut && lut_smem < 2048) lut_smem *= 2;
+        while (lut_smem < max_lut && lut_smem < pvr::kMaxSmemLut) lut_smem *= 2;
         sp.lut_smem_entries = lut_smem;
         const bool smem = sp.job.f.lut_size <= lut_smem;
         const int variant = (sp.job.normals ? pvr::kSingleNormals : 0) | (smem ? pvr::kSingleSmemLut : 0) |
-                            (sp.job.compact ? pvr::kSingleCompact : 0);
+                            (sp.job.compact ? pvr::kSingleCompact : 0) | (fast ? pvr::kSingleFast : 0);
         const long long tiles = (long long)sp.job.tiles_x * sp.job.tiles_y;
         void *args[] = {&sp};
         PVR_CUDA(cudaLaunchKernel(pvr::single_kernel(log2b, b->tuning, variant), dim3((unsigned)tiles),
@@ -187,9 +197,9 @@ int launch_chunk(pvr_batch *b, const pvr_job *jobs, int n, cudaStream_t st) {
     pvr::BatchParams &p = *b->params;
     long long total = 0;
     for (int i = 0; i < n; ++i) {
-        if (int rc = pvr::fill_job(jobs[i], b->tuning.tile_w, b->tuning.tile_h, p.jobs[i])) {
+        if (int rc = pvr::fill_job(jobs[i], b->tuning.tile_w, b->tuning.tile_h, fast, p.jobs[i])) {
             const std::string why = pvr_last_error();
-            return fail(rc, "job %d: %s", i, why.c_str());
+            return fail(rc, "job %d: %s", idx[i], why.c_str());
         }
         p.jobs[i].tile_base = (int)total;
         p.tile_base[i] = (int)total;
@@ -203,14 +213,16 @@ int launch_chunk(pvr_batch *b, const pvr_job *jobs, int n, cudaStream_t st) {
     // LUT staging sized by the largest table (a few fixed sizes so graphs are
     // reused); larger tables are read through the read-only cache
     int lut_smem = 256;
-    while (lut_smem < max_lut && lut_smem < 2048) lut_smem *= 2;
+    while (lut_smem < max_lut && lut_smem < pvr::kMaxSmemLut) lut_smem *= 2;
+    const int variant = pvr::job_variant(p.jobs[0]);
+    if (!(variant & pvr::kSingleSmemLut)) lut_smem = 0;  // the LUTs are read from global memory
     p.lut_smem_entries = lut_smem;
     p.work = s.d_work;
     int per_sm = b->tuning.blocks_per_sm;
-    const int fit = pvr::max_batch_blocks_per_sm(log2b, b->tuning, lut_smem);
+    const int fit = pvr::max_batch_blocks_per_sm(log2b, b->tuning, lut_smem, variant);
     if (per_sm <= 0 || per_sm > fit) per_sm = std::max(1, fit);
     LaunchKey key;
-    key.fn = pvr::batch_kernel(log2b, b->tuning);
+    key.fn = pvr::batch_kernel(log2b, b->tuning, variant);
     key.grid = b->sms * per_sm;
     key.lut_smem = lut_smem;
     void *args[] = {&p};
@@ -300,8 +312,15 @@ int pvr_batch_render(pvr_batch *b, const pvr_job *jobs, int n, void *stream) {
             return fail(PVR_ERR_VALUE, "all volumes of a batch must share one brick size");
     }
     cudaStream_t st = stream ? (cudaStream_t)stream : b->stream;
-    for (int i0 = 0; i0 < n; i0 += pvr::kMaxLaunchJobs)
-        if (int rc = launch_chunk(b, jobs + i0, std::min(pvr::kMaxLaunchJobs, n - i0), st)) return rc;
+    const bool fast = pvr::arithmetic_fast();  // one arithmetic for the whole call
+    // one launch (or more, of at most kMaxLaunchJobs) per kernel variant
+    std::vector<int> groups[16];
+    for (int i = 0; i < n; ++i) groups[pvr::job_variant_of(jobs[i], fast)].push_back(i);
+    for (auto &g : groups)
+        for (size_t i0 = 0; i0 < g.size(); i0 += pvr::kMaxLaunchJobs)
+            if (int rc = launch_chunk(b, jobs, g.data() + i0,
+                                      (int)std::min<size_t>(pvr::kMaxLaunchJobs, g.size() - i0), fast, st))
+                return rc;
     return PVR_OK;
 }
 

@@ -14,9 +14,10 @@
 // (cudaMemsetAsync on the caller's stream) before the launches that use it.
 //
 // Limits and rules:
-//  * at most kStaticCounters launches of kMaxLaunchJobs jobs per call
-//    (64 x 96 = 6144 jobs); larger calls fail with PVR_ERR_VALUE before
-//    anything is queued;
+//  * at most kStaticCounters launches per call, one per kernel variant
+//    (normals, record form, arithmetic) and per kMaxLaunchJobs jobs of it
+//    (64 x 96 = 6144 jobs of one variant); larger calls fail with
+//    PVR_ERR_VALUE before anything is queued;
 //  * the counters are shared by every call on a device: two calls whose work
 //    may overlap on the GPU (different streams, or different host threads
 //    without ordering) race on them and can skip or repeat tiles.  Issue the
@@ -137,49 +138,85 @@ extern "C" int pvr_batch_render_static(const pvr_job *jobs, int n, const pvr_tun
     int *counters = nullptr;
     if (int rc = counters_for_device(device, &counters)) return rc;
     cudaStream_t st = (cudaStream_t)stream;
-    const void *fn = pvr::batch_kernel(log2b, t);
+    const bool fast = pvr::arithmetic_fast();
+    // jobs grouped by kernel variant (counting sort, on the stack): one launch
+    // per variant and per kMaxLaunchJobs jobs, one static counter per launch
+    constexpr int kVariants = 16;
+    int order[kMaxJobs];
+    int start[kVariants + 1] = {0};
+    for (int i = 0; i < n; ++i) ++start[pvr::job_variant_of(jobs[i], fast) + 1];
+    for (int v = 0; v < kVariants; ++v) start[v + 1] += start[v];
+    {
+        int next[kVariants];
+        for (int v = 0; v < kVariants; ++v) next[v] = start[v];
+        for (int i = 0; i < n; ++i) order[next[pvr::job_variant_of(jobs[i], fast)]++] = i;
+    }
+    int launches = 0;
+    for (int v = 0; v < kVariants; ++v)
+        launches += (start[v + 1] - start[v] + pvr::kMaxLaunchJobs - 1) / pvr::kMaxLaunchJobs;
+    if (launches > kStaticCounters)
+        return fail(PVR_ERR_VALUE,
+                    "pvr_batch_render_static: the jobs need %d launches (one per kernel variant and per %d "
+                    "jobs), at most %d per call",
+                    launches, pvr::kMaxLaunchJobs, kStaticCounters);
     // job tables are built on the host stack: the launch copies its parameters
     pvr::BatchParams p;
-    const int launches = (n + pvr::kMaxLaunchJobs - 1) / pvr::kMaxLaunchJobs;
     // validate every job before anything is queued
-    for (int c = 0; c < launches; ++c) {
-        const int i0 = c * pvr::kMaxLaunchJobs, m = std::min(pvr::kMaxLaunchJobs, n - i0);
-        long long total = 0;
-        for (int i = 0; i < m; ++i) {
-            if (int rc = pvr::fill_job(jobs[i0 + i], t.tile_w, t.tile_h, p.jobs[i])) {
-                const std::string why = pvr_last_error();
-                return fail(rc, "job %d: %s", i0 + i, why.c_str());
-            }
-            total += (long long)p.jobs[i].tiles_x * p.jobs[i].tiles_y;
+    for (int i = 0; i < n; ++i) {
+        if (int rc = pvr::fill_job(jobs[i], t.tile_w, t.tile_h, fast, p.jobs[0])) {
+            const std::string why = pvr_last_error();
+            return fail(rc, "job %d: %s", i, why.c_str());
         }
-        if (total > (1LL << 30)) return fail(PVR_ERR_VALUE, "launch %d has too many tiles", c);
+    }
+    for (int v = 0, c = 0; v < kVariants; ++v) {
+        for (int i0 = start[v]; i0 < start[v + 1]; i0 += pvr::kMaxLaunchJobs) {
+            const int m = std::min(pvr::kMaxLaunchJobs, start[v + 1] - i0);
+            long long total = 0;
+            int max_lut = 1;
+            for (int i = 0; i < m; ++i) {
+                const pvr_job &j = jobs[order[i0 + i]];
+                pvr::fill_job(j, t.tile_w, t.tile_h, fast, p.jobs[i]);
+                p.jobs[i].tile_base = (int)total;
+                p.tile_base[i] = (int)total;
+                total += (long long)p.jobs[i].tiles_x * p.jobs[i].tiles_y;
+                max_lut = std::max(max_lut, j.lut->size);
+            }
+            if (total > (1LL << 30)) return fail(PVR_ERR_VALUE, "launch %d has too many tiles", c);
+            ++c;
+        }
     }
     PVR_CUDA(cudaMemsetAsync(counters, 0, (size_t)launches * sizeof(int), st));
-    for (int c = 0; c < launches; ++c) {
-        const int i0 = c * pvr::kMaxLaunchJobs, m = std::min(pvr::kMaxLaunchJobs, n - i0);
-        long long total = 0;
-        int max_lut = 1;
-        for (int i = 0; i < m; ++i) {
-            pvr::fill_job(jobs[i0 + i], t.tile_w, t.tile_h, p.jobs[i]);
-            p.jobs[i].tile_base = (int)total;
-            p.tile_base[i] = (int)total;
-            total += (long long)p.jobs[i].tiles_x * p.jobs[i].tiles_y;
-            max_lut = std::max(max_lut, jobs[i0 + i].lut->size);
+    for (int v = 0, c = 0; v < kVariants; ++v) {
+        if (start[v + 1] == start[v]) continue;
+        const void *fn = pvr::batch_kernel(log2b, t, v);
+        for (int i0 = start[v]; i0 < start[v + 1]; i0 += pvr::kMaxLaunchJobs, ++c) {
+            const int m = std::min(pvr::kMaxLaunchJobs, start[v + 1] - i0);
+            long long total = 0;
+            int max_lut = 1;
+            for (int i = 0; i < m; ++i) {
+                const pvr_job &j = jobs[order[i0 + i]];
+                pvr::fill_job(j, t.tile_w, t.tile_h, fast, p.jobs[i]);
+                p.jobs[i].tile_base = (int)total;
+                p.tile_base[i] = (int)total;
+                total += (long long)p.jobs[i].tiles_x * p.jobs[i].tiles_y;
+                max_lut = std::max(max_lut, j.lut->size);
+            }
+            p.njobs = m;
+            p.total_tiles = (int)total;
+            p.tile_w = t.tile_w;
+            p.tile_h = t.tile_h;
+            int lut_smem = 256;
+            while (lut_smem < max_lut && lut_smem < pvr::kMaxSmemLut) lut_smem *= 2;
+            if (!(v & pvr::kSingleSmemLut)) lut_smem = 0;  // the LUTs are read from global memory
+            p.lut_smem_entries = lut_smem;
+            p.work = counters + c;
+            int per_sm = t.blocks_per_sm;
+            const int fit = pvr::max_batch_blocks_per_sm(log2b, t, lut_smem, v);
+            if (per_sm <= 0 || per_sm > fit) per_sm = std::max(1, fit);
+            void *args[] = {&p};
+            PVR_CUDA(cudaLaunchKernel(fn, dim3(sms * per_sm), dim3(pvr::kBatchThreads), args,
+                                      pvr::batch_smem_bytes(lut_smem), st));
         }
-        p.njobs = m;
-        p.total_tiles = (int)total;
-        p.tile_w = t.tile_w;
-        p.tile_h = t.tile_h;
-        int lut_smem = 256;
-        while (lut_smem < max_lut && lut_smem < 2048) lut_smem *= 2;
-        p.lut_smem_entries = lut_smem;
-        p.work = counters + c;
-        int per_sm = t.blocks_per_sm;
-        const int fit = pvr::max_batch_blocks_per_sm(log2b, t, lut_smem);
-        if (per_sm <= 0 || per_sm > fit) per_sm = std::max(1, fit);
-        void *args[] = {&p};
-        PVR_CUDA(cudaLaunchKernel(fn, dim3(sms * per_sm), dim3(pvr::kBatchThreads), args,
-                                  pvr::batch_smem_bytes(lut_smem), st));
     }
     return PVR_OK;
 }

@@ -30,8 +30,9 @@
 // (lut[i1] - lut[i0]) * lut_size; density = value_scale * trilinear(voxels)
 // gives each of the 8 corners its trilinear weight.  Normals (given, or
 // (density, 0, 0) without a normal volume) are held constant.  LUT gradients
-// are summed in shared memory per block and added to global memory once per
-// block; voxel gradients are added with global atomics.
+// are summed per warp over the lanes that address the same entries, then in
+// shared memory per block, and added to global memory once per block; voxel
+// gradients are added with global atomics.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -46,7 +47,7 @@ namespace {
 constexpr int kDiffMaxViews = 32;   // views per launch (more are split)
 constexpr int kDiffThreads = 256;   // 16 x 16 pixel tile; warps cover 8 x 4 pixels
 constexpr int kDiffTile = 16;
-constexpr int kSeg = 32;            // reverse-march segment (iterations)
+constexpr int kSeg = 16;            // reverse-march segment (iterations), buffered in shared memory
 constexpr int kDiffMaxLut = 2048;   // LUT entries (shared-memory gradient)
 
 struct DiffParams {
@@ -247,8 +248,34 @@ __device__ __forceinline__ void add_voxel_grad(const DiffParams &p, const Sample
         }
 }
 
+// Sums v[0..7] over each group of lanes in `peers` (the lanes of `active`
+// with the same key, from __match_any_sync) by a tree over the group's
+// ranks; returns true on the group's lowest lane, which then holds the sums.
+// Every lane of `active` must call it.
+__device__ __forceinline__ bool reduce_peers(unsigned active, unsigned peers, float v[8]) {
+    const int lane = threadIdx.x & 31;
+    int rank = __popc(peers & ((1u << lane) - 1u));
+    unsigned above = lane == 31 ? 0u : peers & (0xffffffffu << (lane + 1));
+    bool member = true;  // still holds a partial sum of its group
+    while (__any_sync(active, member && above != 0u)) {
+        const int next = (member && above) ? __ffs(above) - 1 : lane;
+        const bool take = member && above != 0u && !(rank & 1);
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            const float t = __shfl_sync(active, v[c], next);
+            if (take) v[c] += t;
+        }
+        // the odd ranks have handed their sums down and leave
+        const unsigned leaving = __ballot_sync(active, member && (rank & 1));
+        if (member && (rank & 1)) member = false;
+        above &= ~leaving;
+        rank >>= 1;
+    }
+    return member;
+}
+
 __device__ void backward_ray(const DiffParams &p, const MarchFrame &f, int px, int py, long long idx,
-                             float *s_glut) {
+                             float *s_glut, float *s_seg) {
     const int nsteps = p.steps[idx];
     if (nsteps <= 0) return;
     const float4 g = p.gimage[idx];
@@ -258,7 +285,9 @@ __device__ void backward_ray(const DiffParams &p, const MarchFrame &f, int px, i
     const float4 out = p.image[idx];
     float T = __fadd_rn(1.0f, -out.w);
     float Rr = 0.0f, Rg = 0.0f, Rb = 0.0f, Ra = 0.0f;
-    float buf[kSeg][3];
+    // this thread's kSeg x 3 positions, strided by the block size (no bank
+    // conflicts between the lanes of a warp)
+    float *seg = s_seg + threadIdx.x;
     int end = nsteps;
     while (end > 0) {
         const int start = max(0, end - kSeg);
@@ -269,13 +298,15 @@ __device__ void backward_ray(const DiffParams &p, const MarchFrame &f, int px, i
         for (int k = start; k < end; ++k) {
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
-                buf[k - start][a] = q[a];
+                seg[((k - start) * 3 + a) * kDiffThreads] = q[a];
                 q[a] = __fadd_rn(q[a], d[a]);
             }
         }
         for (int k = end - 1; k >= start; --k) {
             float t[3];
-            if (!tex_coords(f, buf[k - start], t)) continue;
+            const float bpos[3] = {seg[((k - start) * 3 + 0) * kDiffThreads], seg[((k - start) * 3 + 1) * kDiffThreads],
+                                   seg[((k - start) * 3 + 2) * kDiffThreads]};
+            if (!tex_coords(f, bpos, t)) continue;
             Sample s;
             eval_sample(p, f, t, true, s);
             const float om = 1.0f - s.alpha;
@@ -286,17 +317,21 @@ __device__ void backward_ray(const DiffParams &p, const MarchFrame &f, int px, i
             const float dr = g.x * kc, dg = g.y * kc, db = g.z * kc;
             const float da = dalpha * f.alpha_k * s.e;
             if (s_glut) {
+                // neighbouring rays of a warp mostly address the same LUT
+                // entries: the lanes with the same pair of entries sum their
+                // contributions first, and one lane per pair adds them
                 const float w1 = s.la, w0 = 1.0f - s.la;
-                float *e0 = s_glut + 4 * s.i0;
-                float *e1 = s_glut + 4 * s.i1;
-                atomicAdd(e0 + 0, w0 * dr);
-                atomicAdd(e0 + 1, w0 * dg);
-                atomicAdd(e0 + 2, w0 * db);
-                atomicAdd(e0 + 3, w0 * da);
-                atomicAdd(e1 + 0, w1 * dr);
-                atomicAdd(e1 + 1, w1 * dg);
-                atomicAdd(e1 + 2, w1 * db);
-                atomicAdd(e1 + 3, w1 * da);
+                float v[8] = {w0 * dr, w0 * dg, w0 * db, w0 * da, w1 * dr, w1 * dg, w1 * db, w1 * da};
+                const unsigned active = __activemask();
+                const unsigned peers = __match_any_sync(active, ((unsigned)s.i0 << 16) | (unsigned)s.i1);
+                if (reduce_peers(active, peers, v)) {
+                    const int n = f.lut_size;  // channel-major: s_glut[c * n + entry]
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) {
+                        if (v[c] != 0.0f) atomicAdd(s_glut + c * n + s.i0, v[c]);
+                        if (v[4 + c] != 0.0f) atomicAdd(s_glut + c * n + s.i1, v[4 + c]);
+                    }
+                }
             }
             if (p.gvol) {
                 const float gd = (dr * (s.B.x - s.A.x) + dg * (s.B.y - s.A.y) + db * (s.B.z - s.A.z) +
@@ -313,9 +348,14 @@ __device__ void backward_ray(const DiffParams &p, const MarchFrame &f, int px, i
     }
 }
 
+// Dynamic shared memory: the reverse march's position segments (kSeg x 3
+// floats per thread), then the block's LUT gradient (4 x lut_size floats,
+// channel-major) when the LUT gradient is wanted.
 __global__ void __launch_bounds__(kDiffThreads)
 diff_backward_kernel(const __grid_constant__ DiffParams p) {
-    extern __shared__ float s_glut[];
+    extern __shared__ float s_dyn[];
+    float *s_seg = s_dyn;
+    float *s_glut = s_dyn + kSeg * 3 * kDiffThreads;
     const int lut_floats = 4 * p.f[0].lut_size;
     if (p.glut) {
         for (int k = threadIdx.x; k < lut_floats; k += kDiffThreads) s_glut[k] = 0.0f;
@@ -330,13 +370,14 @@ diff_backward_kernel(const __grid_constant__ DiffParams p) {
         pixel_of(tile % per_view, p.tiles_x, px, py);
         if (px < f.width && py < f.height)
             backward_ray(p, f, px, py, ((long long)view * f.height + py) * f.width + px,
-                         p.glut ? s_glut : nullptr);
+                         p.glut ? s_glut : nullptr, s_seg);
     }
     if (p.glut) {
         __syncthreads();
-        float *g = reinterpret_cast<float *>(p.glut);
+        float *g = reinterpret_cast<float *>(p.glut);  // (lut_size, 4), entry-major
+        const int n = p.f[0].lut_size;
         for (int k = threadIdx.x; k < lut_floats; k += kDiffThreads)
-            if (s_glut[k] != 0.0f) atomicAdd(g + k, s_glut[k]);
+            if (s_glut[k] != 0.0f) atomicAdd(g + 4 * (k % n) + k / n, s_glut[k]);
     }
 }
 
@@ -437,7 +478,12 @@ extern "C" int pvr_diff_backward(const pvr_diff_scene *s, const float *d_image, 
     int device = 0, sms = 0;
     PVR_CUDA(cudaGetDevice(&device));
     PVR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
-    const size_t smem = d_grad_lut ? (size_t)s->lut_size * 4 * sizeof(float) : 0;
+    const size_t smem = (size_t)pvr::kSeg * 3 * pvr::kDiffThreads * sizeof(float) +
+                        (d_grad_lut ? (size_t)s->lut_size * 4 * sizeof(float) : 0);
+    // more than 48 KB of dynamic shared memory (set on the current device)
+    PVR_CUDA(cudaFuncSetAttribute((const void *)pvr::diff_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)(pvr::kSeg * 3 * pvr::kDiffThreads * sizeof(float) +
+                                        pvr::kDiffMaxLut * 4 * sizeof(float))));
     int per_sm = 0;
     PVR_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pvr::diff_backward_kernel, pvr::kDiffThreads,
                                                            smem));

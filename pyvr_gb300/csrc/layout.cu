@@ -2,9 +2,10 @@
 //
 // The reference keeps the voxels and the normals as two 3D textures
 // (pyvr/moderngl_renderer/manager.py:77-135).  Here both are re-laid out
-// once per volume into 16-byte texel records {stored value, nx, ny, nz}
-// (the stored value converted exactly to float; uint8 and float16 keep
-// their values, the scale to density is applied after interpolation),
+// once per volume into texel records {stored value, nx, ny, nz}: 16-byte
+// floats, or 8-byte halves for uint8 and float16 volumes (whose values are
+// halves exactly; the normals are then rounded to half) -- the stored value
+// keeps its value, the scale to density is applied after interpolation --
 // grouped in bricks of (B+1)^3 records for bricks of B^3 texels.  The
 // brick grid is shifted by one texel: brick b holds, at local index l, the
 // texel clamp(b*B - 1 + l, 0, extent - 1) on each axis.  A sample with
@@ -20,6 +21,7 @@
 #include <algorithm>
 #include <vector>
 
+#include "normals.cuh"
 #include "pvr_device.cuh"
 #include "pvr_internal.h"
 
@@ -36,155 +38,114 @@ template <> __device__ __forceinline__ float raw_value<__half>(const __half *p, 
     return __half2float(p[i]);
 }
 
-__device__ __forceinline__ float round_half(float x) { return __half2float(__float2half_rn(x)); }
 
-// Normal of array element (a, b, c) of the (D,H,W) volume, as
-// pyvr/datasets/synthetic.py:109-122 computes it with numpy:
-// g_axis = numpy.gradient along each array axis (central difference / 2
-// inside, one-sided on the two faces, unit spacing), n = |g| + 1e-8 with
-// the squares summed left to right, normal = g / n, cast to float32.
-// numpy evaluates this in float64 for integer input, in float16 (each
-// operation rounded to half, sums accumulated in float) for float16 input,
-// and in float32 for float32 input; so does this function.
-template <typename T> struct GradientArith;
-
-template <> struct GradientArith<float> {
-    static __device__ float3 normal(const float *v, const int dims[3], int a, int b, int c) {
-        float g[3];
-        const int idx[3] = {a, b, c};
-        const long long stride[3] = {(long long)dims[1] * dims[2], dims[2], 1};
-        const long long base = a * stride[0] + b * stride[1] + c;
+// The normal of array element (a, b, c), its neighbours read from global
+// memory.
+template <typename T>
+__device__ float3 normal_global(const T *v, const int dims[3], int a, int b, int c) {
+    const int idx[3] = {a, b, c};
+    const long long stride[3] = {(long long)dims[1] * dims[2], dims[2], 1};
+    const long long base = a * stride[0] + b * stride[1] + c;
+    float g[3];
+    const float v0 = raw_value<T>(v, base);
 #pragma unroll
-        for (int ax = 0; ax < 3; ++ax) {
-            const int i = idx[ax], n = dims[ax];
-            const long long s = stride[ax];
-            if (i == 0) g[ax] = __fsub_rn(v[base + s], v[base]);
-            else if (i == n - 1) g[ax] = __fsub_rn(v[base], v[base - s]);
-            else g[ax] = __fmul_rn(__fsub_rn(v[base + s], v[base - s]), 0.5f);
-        }
-        float ss = __fadd_rn(__fadd_rn(__fmul_rn(g[0], g[0]), __fmul_rn(g[1], g[1])), __fmul_rn(g[2], g[2]));
-        float nrm = __fadd_rn(__fsqrt_rn(ss), 1e-8f);
-        return make_float3(__fdiv_rn(g[0], nrm), __fdiv_rn(g[1], nrm), __fdiv_rn(g[2], nrm));
+    for (int ax = 0; ax < 3; ++ax) {
+        const int i = idx[ax], n = dims[ax];
+        const long long s = stride[ax];
+        const float vm = i > 0 ? raw_value<T>(v, base - s) : 0.0f;
+        const float vp = i < n - 1 ? raw_value<T>(v, base + s) : 0.0f;
+        g[ax] = GradientArith<T>::axis(vm, v0, vp, i, n);
     }
-};
+    return GradientArith<T>::finish(g[0], g[1], g[2]);
+}
 
-template <> struct GradientArith<uint8_t> {
-    static __device__ float3 normal(const uint8_t *v, const int dims[3], int a, int b, int c) {
-        double g[3];
-        const int idx[3] = {a, b, c};
-        const long long stride[3] = {(long long)dims[1] * dims[2], dims[2], 1};
-        const long long base = a * stride[0] + b * stride[1] + c;
-#pragma unroll
-        for (int ax = 0; ax < 3; ++ax) {
-            const int i = idx[ax], n = dims[ax];
-            const long long s = stride[ax];
-            if (i == 0) g[ax] = (double)v[base + s] - (double)v[base];
-            else if (i == n - 1) g[ax] = (double)v[base] - (double)v[base - s];
-            else g[ax] = ((double)v[base + s] - (double)v[base - s]) / 2.0;  // exact
-        }
-        double ss = __dadd_rn(__dadd_rn(__dmul_rn(g[0], g[0]), __dmul_rn(g[1], g[1])), __dmul_rn(g[2], g[2]));
-        double nrm = __dadd_rn(__dsqrt_rn(ss), 1e-8);
-        return make_float3(__double2float_rn(__ddiv_rn(g[0], nrm)), __double2float_rn(__ddiv_rn(g[1], nrm)),
-                           __double2float_rn(__ddiv_rn(g[2], nrm)));
-    }
-};
+template <typename Rec> __device__ __forceinline__ Rec make_record(float v, float3 n);
+template <> __device__ __forceinline__ float4 make_record<float4>(float v, float3 n) {
+    return make_float4(v, n.x, n.y, n.z);
+}
+// {value, nx, ny, nz} as halves, each rounded to nearest
+template <> __device__ __forceinline__ uint2 make_record<uint2>(float v, float3 n) {
+    const uint32_t h0 = __half_as_ushort(__float2half_rn(v)), h1 = __half_as_ushort(__float2half_rn(n.x));
+    const uint32_t h2 = __half_as_ushort(__float2half_rn(n.y)), h3 = __half_as_ushort(__float2half_rn(n.z));
+    return make_uint2(h0 | (h1 << 16), h2 | (h3 << 16));
+}
 
-template <> struct GradientArith<__half> {
-    static __device__ float3 normal(const __half *v, const int dims[3], int a, int b, int c) {
-        float g[3];
-        const int idx[3] = {a, b, c};
-        const long long stride[3] = {(long long)dims[1] * dims[2], dims[2], 1};
-        const long long base = a * stride[0] + b * stride[1] + c;
-#pragma unroll
-        for (int ax = 0; ax < 3; ++ax) {
-            const int i = idx[ax], n = dims[ax];
-            const long long s = stride[ax];
-            if (i == 0) {
-                g[ax] = round_half(__fsub_rn(__half2float(v[base + s]), __half2float(v[base])));
-            } else if (i == n - 1) {
-                g[ax] = round_half(__fsub_rn(__half2float(v[base]), __half2float(v[base - s])));
-            } else {
-                float d = round_half(__fsub_rn(__half2float(v[base + s]), __half2float(v[base - s])));
-                g[ax] = round_half(__fdiv_rn(d, 2.0f));
-            }
-        }
-        // squares rounded to half; the sum accumulates in float, rounds once
-        float q0 = round_half(__fmul_rn(g[0], g[0]));
-        float q1 = round_half(__fmul_rn(g[1], g[1]));
-        float q2 = round_half(__fmul_rn(g[2], g[2]));
-        float ss = round_half(__fadd_rn(__fadd_rn(q0, q1), q2));
-        float nrm = round_half(__fsqrt_rn(ss));  // + 1e-8 rounds to + 0 in half
-        return make_float3(round_half(__fdiv_rn(g[0], nrm)), round_half(__fdiv_rn(g[1], nrm)),
-                           round_half(__fdiv_rn(g[2], nrm)));
-    }
-};
+constexpr int kLayoutThreads = 256;
 
-// One thread per record.  Voxel (x, y, z) along world axes lives at
-// z + D*(y + H*x) of the (D,H,W) C-order buffer (the GL texture of size
-// (D,H,W) read through the z/y/x swizzle, volume.frag.glsl:90); the normal
-// texture is indexed the same way (manager.py:123-125).
-template <typename T, int LOG2B>
-__global__ void build_records_kernel(BrickGeometry g, const T *__restrict__ vol, int D, int H, int W,
-                                     const float *__restrict__ nrm, int normals_mode,
-                                     const uint32_t *__restrict__ table,
-                                     float4 *__restrict__ records) {
-    constexpr int B = 1 << LOG2B, A = B + 1, R = A * A * A;
+// One block per brick (grid-stride over bricks).  The block first stages
+// the brick's texels plus a two-texel margin ((B+3)^3, clamped to the
+// volume) in shared memory, then writes the brick's (B+1)^3 records: the
+// stored value and the normal (given: read from `nrm`; computed on the
+// device: numpy.gradient from the staged neighbours when the volume is
+// cubic -- array axes are then the world axes -- else from global memory),
+// and finally the brick's {slot, min, max} from a block reduction over the
+// records' values (a NaN marks the brick as never skippable).  Voxel
+// (x, y, z) along world axes lives at z + D*(y + H*x) of the (D,H,W) C-order
+// buffer (the GL texture of size (D,H,W) read through the z/y/x swizzle,
+// volume.frag.glsl:90); the normal texture is indexed the same way
+// (manager.py:123-125).  Rec: float4 records, or uint2 half records (only
+// for storage types whose values are halves exactly).
+template <typename T, int LOG2B, typename Rec>
+__global__ void __launch_bounds__(kLayoutThreads)
+build_bricks_kernel(BrickGeometry g, const T *__restrict__ vol, int D, int H, int W,
+                    const float *__restrict__ nrm, int normals_mode, const uint32_t *__restrict__ table,
+                    Rec *__restrict__ records, uint4 *__restrict__ bricks) {
+    constexpr int B = 1 << LOG2B, A = B + 1, R = A * A * A, S = B + 3, S3 = S * S * S;
+    constexpr int WARPS = kLayoutThreads / 32;
+    __shared__ float sv[S3];
+    __shared__ float s_lo[WARPS], s_hi[WARPS];
+    __shared__ int s_nan[WARPS];
     const int dims[3] = {D, H, W};
-    const long long total = (long long)g.nbricks * R;
-    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < total;
-         r += (long long)gridDim.x * blockDim.x) {
-        const int brick = (int)(r / R);
-        const int rec = (int)(r - (long long)brick * R);
+    const bool cubic = D == H && H == W;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int brick = blockIdx.x; brick < g.nbricks; brick += gridDim.x) {
         const int bz = brick % g.nb[2];
         const int by = (brick / g.nb[2]) % g.nb[1];
         const int bx = brick / (g.nb[2] * g.nb[1]);
-        const int lz = rec % A, ly = (rec / A) % A, lx = rec / (A * A);
-        const int x = min(max(bx * B - 1 + lx, 0), g.ext[0] - 1);
-        const int y = min(max(by * B - 1 + ly, 0), g.ext[1] - 1);
-        const int z = min(max(bz * B - 1 + lz, 0), g.ext[2] - 1);
-        const long long src = z + (long long)g.ext[2] * (y + (long long)g.ext[1] * x);
-        float4 v;
-        v.x = raw_value<T>(vol, src);
-        if (normals_mode == PVR_NORMALS_GIVEN) {
-            v.y = nrm[3 * src + 0];
-            v.z = nrm[3 * src + 1];
-            v.w = nrm[3 * src + 2];
-        } else if (normals_mode == PVR_NORMALS_DEVICE) {
-            // array position of flat element `src` in the (D,H,W) array
-            const int c = (int)(src % W);
-            const int b = (int)((src / W) % H);
-            const int a = (int)(src / ((long long)W * H));
-            const float3 n = GradientArith<T>::normal(vol, dims, a, b, c);
-            v.y = n.x;
-            v.z = n.y;
-            v.w = n.z;
-        } else {
-            v.y = v.z = v.w = 0.0f;
+        // staged region: world texels o + r, r in [0, S), o = b*B - 2
+        const int ox = bx * B - 2, oy = by * B - 2, oz = bz * B - 2;
+        for (int i = threadIdx.x; i < S3; i += kLayoutThreads) {
+            const int rz = i % S, ry = (i / S) % S, rx = i / (S * S);
+            const int x = min(max(ox + rx, 0), g.ext[0] - 1);
+            const int y = min(max(oy + ry, 0), g.ext[1] - 1);
+            const int z = min(max(oz + rz, 0), g.ext[2] - 1);
+            sv[i] = raw_value<T>(vol, z + (long long)g.ext[2] * (y + (long long)g.ext[1] * x));
         }
+        __syncthreads();
         const uint32_t slot = table[brick];
-        records[(size_t)slot * R + rec] = v;
-    }
-}
-
-// One warp per brick: min/max of the stored values over all its records
-// (the footprints of every sample that maps to it), stored with the brick's
-// record slot.  A NaN marks the brick as never skippable.
-template <int LOG2B>
-__global__ void brick_minmax_kernel(BrickGeometry g, const uint32_t *__restrict__ table,
-                                    const float4 *__restrict__ records, uint4 *__restrict__ bricks) {
-    constexpr int R = brick_records(LOG2B);
-    const int warps = blockDim.x >> 5;
-    const int lane = threadIdx.x & 31;
-    for (int b = blockIdx.x * warps + (threadIdx.x >> 5); b < g.nbricks; b += gridDim.x * warps) {
-        const uint32_t slot = table[b];
-        const float4 *rp = records + (size_t)slot * R;
         float lo = __int_as_float(0x7f800000), hi = -lo;
         bool nan = false;
-        for (int i = lane; i < R; i += 32) {
-            float v = rp[i].x;
-            nan |= v != v;
-            lo = fminf(lo, v);
-            hi = fmaxf(hi, v);
+        for (int rec = threadIdx.x; rec < R; rec += kLayoutThreads) {
+            const int lz = rec % A, ly = (rec / A) % A, lx = rec / (A * A);
+            // record l of the brick holds texel clamp(b*B - 1 + l)
+            const int x = min(max(bx * B - 1 + lx, 0), g.ext[0] - 1);
+            const int y = min(max(by * B - 1 + ly, 0), g.ext[1] - 1);
+            const int z = min(max(bz * B - 1 + lz, 0), g.ext[2] - 1);
+            const int ri = ((x - ox) * S + (y - oy)) * S + (z - oz);  // in [1, S-2] per axis
+            const float val = sv[ri];
+            nan |= val != val;
+            lo = fminf(lo, val);
+            hi = fmaxf(hi, val);
+            float3 n = make_float3(0.0f, 0.0f, 0.0f);
+            const long long src = z + (long long)g.ext[2] * (y + (long long)g.ext[1] * x);
+            if (normals_mode == PVR_NORMALS_GIVEN) {
+                n = make_float3(nrm[3 * src + 0], nrm[3 * src + 1], nrm[3 * src + 2]);
+            } else if (normals_mode == PVR_NORMALS_DEVICE) {
+                if (cubic) {
+                    // array position (a, b, c) = (x, y, z)
+                    n = GradientArith<T>::finish(
+                        GradientArith<T>::axis(sv[ri - S * S], val, sv[ri + S * S], x, g.ext[0]),
+                        GradientArith<T>::axis(sv[ri - S], val, sv[ri + S], y, g.ext[1]),
+                        GradientArith<T>::axis(sv[ri - 1], val, sv[ri + 1], z, g.ext[2]));
+                } else {
+                    // array position of flat element `src` in the (D,H,W) array
+                    const int c = (int)(src % W);
+                    const int b = (int)((src / W) % H);
+                    const int a = (int)(src / ((long long)W * H));
+                    n = normal_global<T>(vol, dims, a, b, c);
+                }
+            }
+            records[(size_t)slot * R + rec] = make_record<Rec>(val, n);
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
@@ -192,9 +153,23 @@ __global__ void brick_minmax_kernel(BrickGeometry g, const uint32_t *__restrict_
             hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
         }
         nan = __any_sync(0xffffffffu, nan);
-        if (lane == 0)
-            bricks[b] = nan ? make_uint4(slot, 0x7fc00000u, 0u, 0u)
-                            : make_uint4(slot, __float_as_uint(lo), __float_as_uint(hi), 0u);
+        if (lane == 0) {
+            s_lo[warp] = lo;
+            s_hi[warp] = hi;
+            s_nan[warp] = nan;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            bool any_nan = false;
+            for (int w = 0; w < WARPS; ++w) {
+                lo = fminf(lo, s_lo[w]);
+                hi = fmaxf(hi, s_hi[w]);
+                any_nan |= s_nan[w] != 0;
+            }
+            bricks[brick] = any_nan ? make_uint4(slot, 0x7fc00000u, 0u, 0u)
+                                    : make_uint4(slot, __float_as_uint(lo), __float_as_uint(hi), 0u);
+        }
+        __syncthreads();  // sv and the partials are rewritten for the next brick
     }
 }
 
@@ -207,23 +182,27 @@ __device__ __forceinline__ bool half_exact(float x, unsigned short &h) {
     return __float_as_uint(back) == __float_as_uint(x);
 }
 
-// Compact records: {value, nx, ny, nz} as four halves in one 8-byte record.
-// The march decodes them exactly, so a volume whose records all survive the
-// round trip renders the same images from either form.
+// Compact records: {value, nx, ny, nz} as four halves in one 8-byte record,
+// each rounded to nearest.  The march decodes them exactly, so a volume
+// whose records all survive the round trip renders the same images from
+// either form.  *inexact gets bit 0 if some value does not survive it, bit 1
+// if some normal component does not.
 __global__ void compact_records_kernel(const float4 *__restrict__ in, uint2 *__restrict__ out, long long n,
                                        int *__restrict__ inexact) {
-    bool ok = true;
+    unsigned bad = 0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
         const float4 r = in[i];
         unsigned short h0, h1, h2, h3;
-        ok &= half_exact(r.x, h0);
-        ok &= half_exact(r.y, h1);
-        ok &= half_exact(r.z, h2);
-        ok &= half_exact(r.w, h3);
+        const bool v_ok = half_exact(r.x, h0);
+        const bool x_ok = half_exact(r.y, h1);
+        const bool y_ok = half_exact(r.z, h2);
+        const bool z_ok = half_exact(r.w, h3);
+        bad |= (v_ok ? 0u : 1u) | ((x_ok && y_ok && z_ok) ? 0u : 2u);
         out[i] = make_uint2((uint32_t)h0 | ((uint32_t)h1 << 16), (uint32_t)h2 | ((uint32_t)h3 << 16));
     }
-    if (__any_sync(0xffffffffu, !ok) && (threadIdx.x & 31) == 0) atomicExch(inexact, 1);
+    bad = __reduce_or_sync(0xffffffffu, bad);
+    if (bad && (threadIdx.x & 31) == 0) atomicOr(inexact, (int)bad);
 }
 
 __device__ __forceinline__ float4 record_at(const float4 *r, size_t i) { return r[i]; }
@@ -270,31 +249,30 @@ uint32_t spread3(uint32_t v) {  // 10 bits -> every third bit
 
 template <typename T, int LOG2B>
 cudaError_t build_typed(const BrickGeometry &g, const void *vol, const int dims[3], const float *nrm,
-                        int normals_mode, const uint32_t *table, float4 *records, uint4 *bricks,
+                        int normals_mode, const uint32_t *table, void *records, bool half, uint4 *bricks,
                         cudaStream_t st) {
-    constexpr int R = brick_records(LOG2B);
-    const long long total = (long long)g.nbricks * R;
-    int blocks = (int)std::min<long long>((total + 255) / 256, 152LL * 64);
-    build_records_kernel<T, LOG2B><<<blocks, 256, 0, st>>>(g, (const T *)vol, dims[0], dims[1], dims[2],
-                                                          nrm, normals_mode, table, records);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    int mblocks = std::max(1, std::min((g.nbricks + 7) / 8, 152 * 16));
-    brick_minmax_kernel<LOG2B><<<mblocks, 256, 0, st>>>(g, table, records, bricks);
+    const int blocks = std::max(1, std::min(g.nbricks, 152 * 8));
+    if (half)
+        build_bricks_kernel<T, LOG2B, uint2><<<blocks, kLayoutThreads, 0, st>>>(
+            g, (const T *)vol, dims[0], dims[1], dims[2], nrm, normals_mode, table, (uint2 *)records, bricks);
+    else
+        build_bricks_kernel<T, LOG2B, float4><<<blocks, kLayoutThreads, 0, st>>>(
+            g, (const T *)vol, dims[0], dims[1], dims[2], nrm, normals_mode, table, (float4 *)records, bricks);
     return cudaGetLastError();
 }
 
 template <int LOG2B>
 cudaError_t build_log2(const BrickGeometry &g, int dtype, const void *vol, const int dims[3],
-                       const float *nrm, int normals_mode, const uint32_t *table, float4 *records,
+                       const float *nrm, int normals_mode, const uint32_t *table, void *records, bool half,
                        uint4 *bricks, cudaStream_t st) {
     switch (dtype) {
     case PVR_U8:
-        return build_typed<uint8_t, LOG2B>(g, vol, dims, nrm, normals_mode, table, records, bricks, st);
+        return build_typed<uint8_t, LOG2B>(g, vol, dims, nrm, normals_mode, table, records, half, bricks, st);
     case PVR_F16:
-        return build_typed<__half, LOG2B>(g, vol, dims, nrm, normals_mode, table, records, bricks, st);
+        return build_typed<__half, LOG2B>(g, vol, dims, nrm, normals_mode, table, records, half, bricks, st);
     default:
-        return build_typed<float, LOG2B>(g, vol, dims, nrm, normals_mode, table, records, bricks, st);
+        // float32 values are not halves: float records only
+        return build_typed<float, LOG2B>(g, vol, dims, nrm, normals_mode, table, records, false, bricks, st);
     }
 }
 
@@ -330,11 +308,12 @@ std::vector<uint32_t> morton_slots(const BrickGeometry &g) {
 
 cudaError_t launch_build_records(const BrickGeometry &g, int dtype, const void *vol, const int dims[3],
                                  const float *nrm, int normals_mode, const uint32_t *table,
-                                 float4 *records, uint4 *bricks, cudaStream_t st) {
+                                 void *records, bool half, uint4 *bricks, cudaStream_t st) {
+    if (half && dtype == PVR_F32) return cudaErrorInvalidValue;
     switch (g.log2b) {
-    case 2: return build_log2<2>(g, dtype, vol, dims, nrm, normals_mode, table, records, bricks, st);
-    case 4: return build_log2<4>(g, dtype, vol, dims, nrm, normals_mode, table, records, bricks, st);
-    default: return build_log2<3>(g, dtype, vol, dims, nrm, normals_mode, table, records, bricks, st);
+    case 2: return build_log2<2>(g, dtype, vol, dims, nrm, normals_mode, table, records, half, bricks, st);
+    case 4: return build_log2<4>(g, dtype, vol, dims, nrm, normals_mode, table, records, half, bricks, st);
+    default: return build_log2<3>(g, dtype, vol, dims, nrm, normals_mode, table, records, half, bricks, st);
     }
 }
 

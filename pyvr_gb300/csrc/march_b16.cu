@@ -3,12 +3,12 @@
 
 namespace pvr {
 
-const void *batch_kernel_b4(const Tuning &t) { return batch_kernel_log2<4>(t); }
+const void *batch_kernel_b4(const Tuning &t, int variant) { return batch_kernel_log2<4>(t, variant); }
 
 const void *single_kernel_b4(const Tuning &t, int variant) { return single_kernel_log2<4>(t, variant); }
 
-int max_batch_blocks_b4(const Tuning &t, int lut_smem_entries) {
-    return max_blocks_log2<4>(t, lut_smem_entries);
+int max_batch_blocks_b4(const Tuning &t, int lut_smem_entries, int variant) {
+    return max_blocks_log2<4>(t, lut_smem_entries, variant);
 }
 
 }  // namespace pvr

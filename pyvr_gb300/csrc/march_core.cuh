@@ -31,9 +31,21 @@
 //    a sample lies in the brick's value range, and the scale and the LUT
 //    coordinate are monotone float operations evaluated as for a sample.
 //
-// A volume's records are 16-byte floats, or 8-byte halves when every float
-// of them is a half exactly (layout.cu); the half form decodes to the same
-// floats, so the arithmetic, and every output bit, is the same.
+// A volume's records are 16-byte floats, or 8-byte halves (layout.cu); the
+// half form decodes to floats, so the arithmetic is the same either way.
+//
+// Two arithmetics (pvr_set_arithmetic), chosen per launch:
+//  - exact: every operation rounded as the CPU oracle rounds it (no FMA
+//    contraction except the texture lerps, exp by pvr_expf, a correctly
+//    rounded rsqrt), so a frame equals the oracle's bit for bit;
+//  - fast (the default): the position recurrence, the validity test, the
+//    texture addressing, the lerps and the LUT addressing are the exact
+//    arithmetic's, so the same samples are taken from the same texels; the
+//    shading tail fuses products into FMAs, takes exp(-x) as one hardware
+//    ex2 of x*log2(e) and 1/|n| as one hardware rsqrt (relative errors
+//    about 2^-22), and dots n with the light before scaling by 1/|n|.  The
+//    images stay within 1 LSB per RGBA8 channel of the exact ones (tested
+//    at the configurations' full sizes).
 #pragma once
 
 #include "pvr_device.cuh"
@@ -81,13 +93,14 @@ __device__ __forceinline__ int prefix_entry(const int *p, int i) {
 
 // LUT entry index of density d: floor(d*size - 0.5) clamped to the table,
 // as texture(transfer_function_lut, vec2(d, 0.5)) addresses it (frag:96).
-__device__ __forceinline__ int lut_index(float fl, float lmax, int size) {
-    return !(fl >= 0.0f) ? 0 : (fl > lmax ? size - 1 : (int)fl);
+// fl = floor(coordinate); NaN and negative coordinates give entry 0.
+__device__ __forceinline__ int lut_index(float fl, float lmax) {
+    return (int)fminf(fmaxf(fl, 0.0f), lmax);
 }
 
 // Shading + compositing of one in-box sample (frag:93-115).  p: the record
 // of the footprint's lower corner; fx, fy, fz: the filter fractions.
-template <int LOG2B, bool NORMALS, bool SMEM_LUT, typename Rec>
+template <int LOG2B, bool NORMALS, bool SMEM_LUT, bool FAST, typename Rec>
 __device__ __forceinline__ void shade_sample(const MarchFrame &f, const Rec *__restrict__ p,
                                              float fx, float fy, float fz, const float4 *lut,
                                              float2 &acc_rg, float2 &acc_ba) {
@@ -133,18 +146,33 @@ __device__ __forceinline__ void shade_sample(const MarchFrame &f, const Rec *__r
         n[2] = 0.0f;
     }
 
-    // texture(transfer_function_lut, vec2(density, 0.5)) (frag:96)
-    const float lu = __fadd_rn(__fmul_rn(density, f.flut_size), -0.5f);
+    // texture(transfer_function_lut, vec2(density, 0.5)) (frag:96): entries
+    // floor(lu) and floor(lu) + 1, each clamped to the table, and the lerp
+    // weight lu - floor(lu)
+    const float lu = FAST ? fmaf(density, f.flut_size, -0.5f) : __fadd_rn(__fmul_rn(density, f.flut_size), -0.5f);
     const float lfl = floorf(lu);
     const float la = __fadd_rn(lu, -lfl);
-    const float lmax = (float)(f.lut_size - 1);
-    const int i0 = lut_index(lfl, lmax, f.lut_size);
-    // = lut_index(lfl + 1): the next entry from lfl >= 0 on, clamped to the
-    // table (NaN and negative coordinates stay on entry 0)
-    const int i1 = min(i0 + (lfl >= 0.0f ? 1 : 0), f.lut_size - 1);
+    const int i0 = lut_index(lfl, f.flut_max);
+    const int i1 = lut_index(__fadd_rn(lfl, 1.0f), f.flut_max);
     const float4 A = lut_entry<SMEM_LUT>(lut, i0), B = lut_entry<SMEM_LUT>(lut, i1);
     const float2 crg = lerp_tex2(lo2(A), lo2(B), la);
     const float2 cba = lerp_tex2(hi2(A), hi2(B), la);  // (blue, alpha_tf)
+
+    if (FAST) {
+        // alpha = 1 - exp(-alpha_tf * step/ref) (frag:101)
+        const float alpha = __fadd_rn(1.0f, -ex2_approx(-__fmul_rn(cba.y, f.alpha_k2)));
+        // Lambert term (frag:107-110): dot(n, L) / |n|; a zero (or NaN)
+        // normal gives 0
+        const float n2 = fmaf(n[0], n[0], fmaf(n[1], n[1], __fmul_rn(n[2], n[2])));
+        const float dl = fmaf(n[0], f.light_dir[0], fmaf(n[1], f.light_dir[1], __fmul_rn(n[2], f.light_dir[2])));
+        const float di = n2 > 0.0f ? fmaxf(__fmul_rn(dl, rsqrt_approx(n2)), 0.0f) : 0.0f;
+        const float la_ = __fmul_rn(fmaf(f.diffuse, di, f.ambient), alpha);
+        // front-to-back compositing (frag:112-115)
+        const float2 tr = dup2(__fadd_rn(1.0f, -acc_ba.y));
+        acc_rg = __ffma2_rn(tr, __fmul2_rn(crg, dup2(la_)), acc_rg);
+        acc_ba = __ffma2_rn(tr, make_float2(__fmul_rn(cba.x, la_), alpha), acc_ba);
+        return;
+    }
 
     // Beer-Lambert opacity correction (frag:101)
     const float alpha = __fadd_rn(1.0f, -pvr_expf(-__fmul_rn(cba.y, f.alpha_k)));
@@ -185,21 +213,23 @@ __device__ __forceinline__ uint32_t blend_rgba8(float2 rg, float2 ba) {
 
 // Is a sample of this brick exactly transparent under the job's LUT?
 // m = the brick's (min, max) stored values.
-template <bool SMEM_LUT>
+template <bool SMEM_LUT, bool FAST>
 __device__ __forceinline__ bool brick_clear(const MarchFrame &f, float2 m, const int *prefix) {
     if (!(m.x == m.x)) return false;  // NaN in the brick
     const float d0 = __fmul_rn(m.x, f.value_scale), d1 = __fmul_rn(m.y, f.value_scale);
     const float dlo = fminf(d0, d1), dhi = fmaxf(d0, d1);
     if (!(dlo == dlo && dhi == dhi)) return false;
-    const float lmax = (float)(f.lut_size - 1);
-    const int ilo = lut_index(floorf(__fadd_rn(__fmul_rn(dlo, f.flut_size), -0.5f)), lmax, f.lut_size);
-    const int ihi = lut_index(__fadd_rn(floorf(__fadd_rn(__fmul_rn(dhi, f.flut_size), -0.5f)), 1.0f),
-                              lmax, f.lut_size);
+    // the LUT coordinates of the extreme densities, rounded as the march
+    // rounds them (FAST: one FMA); both roundings are monotone in d
+    const float clo = FAST ? fmaf(dlo, f.flut_size, -0.5f) : __fadd_rn(__fmul_rn(dlo, f.flut_size), -0.5f);
+    const float chi = FAST ? fmaf(dhi, f.flut_size, -0.5f) : __fadd_rn(__fmul_rn(dhi, f.flut_size), -0.5f);
+    const int ilo = lut_index(floorf(clo), f.flut_max);
+    const int ihi = lut_index(__fadd_rn(floorf(chi), 1.0f), f.flut_max);
     return prefix_entry<SMEM_LUT>(prefix, ihi + 1) == prefix_entry<SMEM_LUT>(prefix, ilo);
 }
 
 // One pixel's ray of volume.frag.glsl:main (lines 70-122).
-template <int LOG2B, int UNROLL, bool NORMALS, bool SMEM_LUT, bool COMPACT>
+template <int LOG2B, int UNROLL, bool NORMALS, bool SMEM_LUT, bool COMPACT, bool FAST>
 __device__ __forceinline__ void march_ray(const JobDesc &job, int px, int py, const float4 *lut,
                                           const int *prefix, float2 &acc_rg, float2 &acc_ba,
                                           unsigned &n_inbox, unsigned &n_shaded) {
@@ -248,15 +278,16 @@ __device__ __forceinline__ void march_ray(const JobDesc &job, int px, int py, co
                     const uint4 bi = __ldg(job.bricks + id);
                     bp = static_cast<const Rec *>(job.records) + (size_t)bi.x * RECS;
                     clear = job.skip &&
-                            brick_clear<SMEM_LUT>(f, make_float2(__uint_as_float(bi.y), __uint_as_float(bi.z)),
-                                                  prefix);
+                            brick_clear<SMEM_LUT, FAST>(f, make_float2(__uint_as_float(bi.y),
+                                                                       __uint_as_float(bi.z)),
+                                                        prefix);
                 }
                 if (!clear) {
                     ++n_shaded;
                     const int j = (kx & (B - 1)) * SLICE + (ky & (B - 1)) * ROW + (kz & (B - 1));
-                    shade_sample<LOG2B, NORMALS, SMEM_LUT>(f, bp + j, __fadd_rn(ux, -flx),
-                                                           __fadd_rn(uy, -fly), __fadd_rn(uz, -flz),
-                                                           lut, acc_rg, acc_ba);
+                    shade_sample<LOG2B, NORMALS, SMEM_LUT, FAST>(f, bp + j, __fadd_rn(ux, -flx),
+                                                                 __fadd_rn(uy, -fly), __fadd_rn(uz, -flz),
+                                                                 lut, acc_rg, acc_ba);
                 }
             } else {
                 const bool never = entered || (txy.x < 0.0f && dxy.x <= 0.0f) ||
@@ -274,15 +305,15 @@ __device__ __forceinline__ void march_ray(const JobDesc &job, int px, int py, co
     }
 }
 
-template <int LOG2B, int UNROLL, bool NORMALS, bool SMEM_LUT, bool COMPACT>
+template <int LOG2B, int UNROLL, bool NORMALS, bool SMEM_LUT, bool COMPACT, bool FAST>
 __device__ __forceinline__ void march_tile(const JobDesc &job, int px, int py, const float4 *lut,
                                            const int *prefix, int lane) {
     const bool in_image = px < job.f.width && py < job.f.height;
     float2 acc_rg = make_float2(0.0f, 0.0f), acc_ba = make_float2(0.0f, 0.0f);
     unsigned n_inbox = 0, n_shaded = 0;
     if (in_image)
-        march_ray<LOG2B, UNROLL, NORMALS, SMEM_LUT, COMPACT>(job, px, py, lut, prefix, acc_rg, acc_ba,
-                                                             n_inbox, n_shaded);
+        march_ray<LOG2B, UNROLL, NORMALS, SMEM_LUT, COMPACT, FAST>(job, px, py, lut, prefix, acc_rg, acc_ba,
+                                                                   n_inbox, n_shaded);
     if (in_image) {
         const long long idx = (long long)py * job.f.width + px;
         if (job.out8) job.out8[idx] = blend_rgba8(acc_rg, acc_ba);
@@ -302,32 +333,15 @@ __device__ __forceinline__ void march_tile(const JobDesc &job, int px, int py, c
     }
 }
 
-// The job's variant of march_tile: normals or not, LUT staged in shared
-// memory or read from global memory, float or half records.
-template <int LOG2B, int UNROLL, bool COMPACT>
-__device__ __forceinline__ void march_tile_rec(const JobDesc &job, int px, int py, bool lut_in_smem,
-                                               const float4 *s_lut, const int *s_prefix, int lane) {
-    if (job.normals) {
-        if (lut_in_smem) march_tile<LOG2B, UNROLL, true, true, COMPACT>(job, px, py, s_lut, s_prefix, lane);
-        else march_tile<LOG2B, UNROLL, true, false, COMPACT>(job, px, py, job.lut, job.prefix, lane);
-    } else {
-        if (lut_in_smem) march_tile<LOG2B, UNROLL, false, true, COMPACT>(job, px, py, s_lut, s_prefix, lane);
-        else march_tile<LOG2B, UNROLL, false, false, COMPACT>(job, px, py, job.lut, job.prefix, lane);
-    }
-}
-
-template <int LOG2B, int UNROLL>
-__device__ __forceinline__ void march_tile_any(const JobDesc &job, int px, int py, bool lut_in_smem,
-                                               const float4 *s_lut, const int *s_prefix, int lane) {
-    if (job.compact) march_tile_rec<LOG2B, UNROLL, true>(job, px, py, lut_in_smem, s_lut, s_prefix, lane);
-    else march_tile_rec<LOG2B, UNROLL, false>(job, px, py, lut_in_smem, s_lut, s_prefix, lane);
-}
-
-// Persistent batch kernel.  The job table is the kernel's own parameter
-// block (read through the constant cache).  Dynamic shared memory:
-// p.lut_smem_entries float4 LUT entries followed by as many + 1 prefix counts.
-template <int LOG2B, int UNROLL>
-__global__ void __launch_bounds__(kBatchThreads, 5)
+// Persistent batch kernel of one variant: normals or not, LUT staged in
+// shared memory or read from global memory, float or half records, exact or
+// fast arithmetic (the launcher groups a batch's jobs by variant, so that
+// each kernel carries one march and stays within its register budget).  The
+// job table is the kernel's own parameter block (read through the constant
+// cache).  Dynamic shared memory (SMEM_LUT): p.lut_smem_entries float4 LUT
+// entries followed by as many + 1 prefix counts, at least every job's LUT.
+template <int LOG2B, int UNROLL, bool NORMALS, bool SMEM_LUT, bool COMPACT, bool FAST>
+__global__ void __launch_bounds__(kBatchThreads, COMPACT ? 5 : 4)
 march_batch_kernel(const __grid_constant__ BatchParams p) {
     extern __shared__ float4 s_dyn[];
     float4 *s_lut = s_dyn;
@@ -338,7 +352,6 @@ march_batch_kernel(const __grid_constant__ BatchParams p) {
     const int sub_x = (warp % warps_x) * 8 + (lane & 7);
     const int sub_y = (warp / warps_x) * 4 + (lane >> 3);
     int cur_job = -1;
-    bool lut_in_smem = false;
     for (;;) {
         if (threadIdx.x == 0) {
             const int t = atomicAdd(p.work, 1);
@@ -354,21 +367,19 @@ march_batch_kernel(const __grid_constant__ BatchParams p) {
         const int t = s_tile, j = s_job_idx;
         if (t >= p.total_tiles) break;
         const JobDesc &job = p.jobs[j];
-        if (j != cur_job) {
+        if (SMEM_LUT && j != cur_job) {
             // stage the job's LUT (the previous tile's readers passed the
             // barrier at the end of the last round)
-            lut_in_smem = job.f.lut_size <= p.lut_smem_entries;
-            if (lut_in_smem) {
-                for (int k = threadIdx.x; k < job.f.lut_size; k += kBatchThreads) s_lut[k] = job.lut[k];
-                for (int k = threadIdx.x; k <= job.f.lut_size; k += kBatchThreads) s_prefix[k] = job.prefix[k];
-            }
+            for (int k = threadIdx.x; k < job.f.lut_size; k += kBatchThreads) s_lut[k] = job.lut[k];
+            for (int k = threadIdx.x; k <= job.f.lut_size; k += kBatchThreads) s_prefix[k] = job.prefix[k];
             __syncthreads();
             cur_job = j;
         }
         const int local = t - job.tile_base;
         const int px = (local % job.tiles_x) * p.tile_w + sub_x;
         const int py = (local / job.tiles_x) * p.tile_h + sub_y;
-        march_tile_any<LOG2B, UNROLL>(job, px, py, lut_in_smem, s_lut, s_prefix, lane);
+        march_tile<LOG2B, UNROLL, NORMALS, SMEM_LUT, COMPACT, FAST>(job, px, py, SMEM_LUT ? s_lut : job.lut,
+                                                                    SMEM_LUT ? s_prefix : job.prefix, lane);
         __syncthreads();  // s_tile / the staged LUT are rewritten next round
     }
 }
@@ -376,11 +387,11 @@ march_batch_kernel(const __grid_constant__ BatchParams p) {
 // Single-job kernel: one block per tile of one render; the job descriptor
 // is the parameter block itself (static offsets), as in a plain frame kernel.
 // One instantiation per variant (normals, LUT in shared memory, half
-// records), chosen on the host: each gets its own register allocation.
-// SMEM_LUT requires job.f.lut_size <= p.lut_smem_entries.  Half records
-// need 16 fewer registers for a sample's 8 records: those variants run 6
-// blocks per SM (40 registers) instead of 5 (48).
-template <int LOG2B, int UNROLL, bool NORMALS, bool SMEM_LUT, bool COMPACT>
+// records, arithmetic), chosen on the host: each gets its own register
+// allocation.  SMEM_LUT requires job.f.lut_size <= p.lut_smem_entries.  Half
+// records need 16 fewer registers for a sample's 8 records: those variants
+// run 6 blocks per SM (40 registers) instead of 5 (48).
+template <int LOG2B, int UNROLL, bool NORMALS, bool SMEM_LUT, bool COMPACT, bool FAST>
 __global__ void __launch_bounds__(kBatchThreads, COMPACT ? 6 : 5)
 march_single_kernel(const __grid_constant__ SingleParams p) {
     extern __shared__ float4 s_dyn[];
@@ -397,22 +408,27 @@ march_single_kernel(const __grid_constant__ SingleParams p) {
     const int t = blockIdx.x;
     const int px = (t % job.tiles_x) * p.tile_w + (warp % warps_x) * 8 + (lane & 7);
     const int py = (t / job.tiles_x) * p.tile_h + (warp / warps_x) * 4 + (lane >> 3);
-    march_tile<LOG2B, UNROLL, NORMALS, SMEM_LUT, COMPACT>(job, px, py, SMEM_LUT ? s_lut : job.lut,
-                                                          SMEM_LUT ? s_prefix : job.prefix, lane);
+    march_tile<LOG2B, UNROLL, NORMALS, SMEM_LUT, COMPACT, FAST>(job, px, py, SMEM_LUT ? s_lut : job.lut,
+                                                                SMEM_LUT ? s_prefix : job.prefix, lane);
+}
+
+template <int LOG2B, int UNROLL, bool FAST>
+const void *single_variant_of(int v) {
+    switch (v & 7) {
+    case 0: return (const void *)march_single_kernel<LOG2B, UNROLL, false, false, false, FAST>;
+    case 1: return (const void *)march_single_kernel<LOG2B, UNROLL, true, false, false, FAST>;
+    case 2: return (const void *)march_single_kernel<LOG2B, UNROLL, false, true, false, FAST>;
+    case 3: return (const void *)march_single_kernel<LOG2B, UNROLL, true, true, false, FAST>;
+    case 4: return (const void *)march_single_kernel<LOG2B, UNROLL, false, false, true, FAST>;
+    case 5: return (const void *)march_single_kernel<LOG2B, UNROLL, true, false, true, FAST>;
+    case 6: return (const void *)march_single_kernel<LOG2B, UNROLL, false, true, true, FAST>;
+    default: return (const void *)march_single_kernel<LOG2B, UNROLL, true, true, true, FAST>;
+    }
 }
 
 template <int LOG2B, int UNROLL>
 const void *single_variant(int v) {
-    switch (v & 7) {
-    case 0: return (const void *)march_single_kernel<LOG2B, UNROLL, false, false, false>;
-    case 1: return (const void *)march_single_kernel<LOG2B, UNROLL, true, false, false>;
-    case 2: return (const void *)march_single_kernel<LOG2B, UNROLL, false, true, false>;
-    case 3: return (const void *)march_single_kernel<LOG2B, UNROLL, true, true, false>;
-    case 4: return (const void *)march_single_kernel<LOG2B, UNROLL, false, false, true>;
-    case 5: return (const void *)march_single_kernel<LOG2B, UNROLL, true, false, true>;
-    case 6: return (const void *)march_single_kernel<LOG2B, UNROLL, false, true, true>;
-    default: return (const void *)march_single_kernel<LOG2B, UNROLL, true, true, true>;
-    }
+    return (v & kSingleFast) ? single_variant_of<LOG2B, UNROLL, true>(v) : single_variant_of<LOG2B, UNROLL, false>(v);
 }
 
 template <int LOG2B>
@@ -421,16 +437,35 @@ const void *single_kernel_log2(const Tuning &t, int variant) {
     return single_variant<LOG2B, 1>(variant);
 }
 
-template <int LOG2B>
-const void *batch_kernel_log2(const Tuning &t) {
-    if (t.steps_per_iter >= 4) return (const void *)march_batch_kernel<LOG2B, 4>;
-    return (const void *)march_batch_kernel<LOG2B, 1>;
+template <int LOG2B, int UNROLL, bool FAST>
+const void *batch_variant_of(int v) {
+    switch (v & 7) {
+    case 0: return (const void *)march_batch_kernel<LOG2B, UNROLL, false, false, false, FAST>;
+    case 1: return (const void *)march_batch_kernel<LOG2B, UNROLL, true, false, false, FAST>;
+    case 2: return (const void *)march_batch_kernel<LOG2B, UNROLL, false, true, false, FAST>;
+    case 3: return (const void *)march_batch_kernel<LOG2B, UNROLL, true, true, false, FAST>;
+    case 4: return (const void *)march_batch_kernel<LOG2B, UNROLL, false, false, true, FAST>;
+    case 5: return (const void *)march_batch_kernel<LOG2B, UNROLL, true, false, true, FAST>;
+    case 6: return (const void *)march_batch_kernel<LOG2B, UNROLL, false, true, true, FAST>;
+    default: return (const void *)march_batch_kernel<LOG2B, UNROLL, true, true, true, FAST>;
+    }
+}
+
+template <int LOG2B, int UNROLL>
+const void *batch_variant(int v) {
+    return (v & kSingleFast) ? batch_variant_of<LOG2B, UNROLL, true>(v) : batch_variant_of<LOG2B, UNROLL, false>(v);
 }
 
 template <int LOG2B>
-int max_blocks_log2(const Tuning &t, int lut_smem_entries) {
+const void *batch_kernel_log2(const Tuning &t, int variant) {
+    if (t.steps_per_iter >= 4) return batch_variant<LOG2B, 4>(variant);
+    return batch_variant<LOG2B, 1>(variant);
+}
+
+template <int LOG2B>
+int max_blocks_log2(const Tuning &t, int lut_smem_entries, int variant) {
     int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel_log2<LOG2B>(t), kBatchThreads,
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel_log2<LOG2B>(t, variant), kBatchThreads,
                                                   batch_smem_bytes(lut_smem_entries));
     return n;
 }

@@ -34,6 +34,8 @@ struct MarchFrame {
     float value_scale;  // stored voxel value -> density
     int lut_size;
     float flut_size;
+    float flut_max;     // lut_size - 1
+    float alpha_k2;     // alpha_k * log2(e), for exp(-x) = 2^(-x log2 e) (fast arithmetic)
 };
 
 __device__ __forceinline__ float lerp_tex(float a, float b, float t) {
@@ -71,6 +73,20 @@ __device__ __forceinline__ float pvr_expf(float x) {
     // two halves.  Either way the only rounding is that of the final product.
     if (k <= 127) return p * __int_as_float((k + 127) << 23);
     return (p * __int_as_float((64 + 127) << 23)) * __int_as_float((k - 64 + 127) << 23);
+}
+
+// The fast arithmetic's two special functions, each one hardware
+// instruction (PTX ISA: ex2.approx, rsqrt.approx; relative error about
+// 2^-22).  ex2 flushes subnormal results to 0; rsqrt keeps subnormal inputs.
+__device__ __forceinline__ float ex2_approx(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rsqrt_approx(float x) {
+    float y;
+    asm("rsqrt.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
 }
 
 // Ray of pixel (px, py), py counted from the bottom row: vertex-stage uv at

@@ -39,9 +39,10 @@ std::vector<uint32_t> morton_slots(const BrickGeometry &g);
 // device from the stored values (numpy.gradient semantics).
 // bricks[b] = {record slot, min, max (float bits), 0}: what the march needs
 // when a ray enters brick b, in one 16-byte load.
+// half: 8-byte half records (uint8 / float16 volumes only).
 cudaError_t launch_build_records(const BrickGeometry &g, int dtype, const void *vol, const int dims[3],
                                  const float *nrm, int normals_mode, const uint32_t *table,
-                                 float4 *records, uint4 *bricks, cudaStream_t st);
+                                 void *records, bool half, uint4 *bricks, cudaStream_t st);
 cudaError_t launch_read_normals(const BrickGeometry &g, const int dims[3], const uint32_t *table,
                                 const void *records, bool compact, float *out, cudaStream_t st);
 // Half-precision copy of n records ({value, nx, ny, nz} as four halves, 8
@@ -64,7 +65,8 @@ struct JobDesc {
     int normals;
     int skip;  // empty-space test on: the LUT has a clear entry and the light terms are finite
     int compact;  // 8-byte half records
-    int pad_[3];
+    int fast;     // fast arithmetic (see pvr_set_arithmetic)
+    int pad_[2];
 };
 
 // Kernel parameters of one persistent launch: up to kMaxLaunchJobs job
@@ -99,14 +101,24 @@ struct Tuning {
     int blocks_per_sm = 4;
 };
 
-// Persistent batch march (march_core.cuh), one instantiation per brick size:
-// the kernel function for a tuning, and the blocks of it that fit on an SM.
-const void *batch_kernel(int log2b, const Tuning &t);
-// variant bits of the single-job kernel
-constexpr int kSingleNormals = 1, kSingleSmemLut = 2, kSingleCompact = 4;
+// March kernels (march_core.cuh), one instantiation per brick size and
+// variant.  Variant bits: normals, LUT staged in shared memory, half
+// records, fast arithmetic.  The batch kernel function for a tuning and
+// variant, the blocks of it that fit on an SM, and the single-job kernel.
+constexpr int kSingleNormals = 1, kSingleSmemLut = 2, kSingleCompact = 4, kSingleFast = 8;
+// LUTs up to this many entries are staged in shared memory
+constexpr int kMaxSmemLut = 2048;
+const void *batch_kernel(int log2b, const Tuning &t, int variant);
 const void *single_kernel(int log2b, const Tuning &t, int variant);
 size_t batch_smem_bytes(int lut_smem_entries);
-int max_batch_blocks_per_sm(int log2b, const Tuning &t, int lut_smem_entries);
+int max_batch_blocks_per_sm(int log2b, const Tuning &t, int lut_smem_entries, int variant);
+// the variant bits of a job before it is filled
+int job_variant_of(const pvr_job &j, bool fast);
+// the variant bits of a filled job
+inline int job_variant(const JobDesc &j) {
+    return (j.normals ? kSingleNormals : 0) | (j.f.lut_size <= kMaxSmemLut ? kSingleSmemLut : 0) |
+           (j.compact ? kSingleCompact : 0) | (j.fast ? kSingleFast : 0);
+}
 
 }  // namespace pvr
 
@@ -128,7 +140,8 @@ struct pvr_volume {
     pvr::BrickGeometry geo = {};
     void *d_records = nullptr;  // float4 records, or uint2 when compact
     size_t records_bytes = 0;
-    bool compact = false;       // records stored as halves (every float survived exactly)
+    bool compact = false;       // records stored as halves
+    bool compact_exact = true;  // ... and every float of them survived exactly
     uint32_t *d_table = nullptr;  // brick -> record slot
     uint4 *d_bricks = nullptr;    // brick -> {slot, min, max}
     bool layout_ready = false;
@@ -147,13 +160,15 @@ namespace pvr {
 int fail(int code, const char *fmt, ...);
 int cuda_fail(cudaError_t e, const char *what);
 int ensure_volume_layout(pvr_volume *v, cudaStream_t st);
-int try_compact_records(pvr_volume *v, cudaStream_t st);
+int try_compact_records(pvr_volume *v, cudaStream_t st, bool round_normals);
 cudaError_t vol_alloc(void **p, size_t bytes, cudaStream_t st);
 void vol_free(void *p, cudaStream_t st);
 void free_volume_buffers(pvr_volume *v, cudaStream_t st);
 bool invert_gl(const float gl[16], double inv[16]);
 void light_direction(const float pos[3], const float target[3], float out[3]);
-int fill_job(const pvr_job &j, int tile_w, int tile_h, JobDesc &out);
+int fill_job(const pvr_job &j, int tile_w, int tile_h, bool fast, JobDesc &out);
+// the arithmetic renders use (pvr_set_arithmetic): true = fast (default)
+bool arithmetic_fast();
 }  // namespace pvr
 
 #define PVR_CUDA(expr)                                                  \

@@ -115,12 +115,17 @@ void free_volume_buffers(pvr_volume *v, cudaStream_t st) {
     v->d_bricks = nullptr;
 }
 
-// Whether layouts built from now on may use 8-byte half records
-// (pvr_set_compact_records).  Off by default: the decode costs more issue
-// slots than the halved record bytes save while a volume's working set is
-// cached (9 % slower on 256^3 float16 at 1024^2), and gains about 2 % on a
-// serving mix of 128^3-512^3 volumes; it always halves the records' memory.
-static std::atomic<int> g_compact_records{0};
+// Which layouts built from now on use 8-byte half records
+// (pvr_set_compact_records): PVR_RECORDS_FLOAT never, PVR_RECORDS_HALF_EXACT
+// when every value and normal component is a half exactly,
+// PVR_RECORDS_HALF_NORMALS when every value is (uint8 and float16 volumes),
+// normals rounded to half.
+static std::atomic<int> g_compact_records{PVR_RECORDS_FLOAT};
+
+// The arithmetic of renders queued from now on (pvr_set_arithmetic).
+static std::atomic<int> g_arithmetic{PVR_ARITH_FAST};
+
+bool arithmetic_fast() { return g_arithmetic.load(std::memory_order_relaxed) == PVR_ARITH_FAST; }
 
 // Records, brick table and value ranges of a volume (once per volume).
 int ensure_volume_layout(pvr_volume *v, cudaStream_t st) {
@@ -135,30 +140,42 @@ int ensure_volume_layout(pvr_volume *v, cudaStream_t st) {
     v->geo = make_brick_geometry(v->dims, v->log2b);
     std::vector<uint32_t> table = morton_slots(v->geo);
     const size_t nrec = (size_t)v->geo.nbricks * brick_records(v->log2b);
-    PVR_CUDA(vol_alloc((void **)&v->d_records, nrec * sizeof(float4), st));
-    v->records_bytes = nrec * sizeof(float4);
+    const int mode = g_compact_records.load();
+    // half records written directly: values of uint8 / float16 volumes are
+    // halves exactly; normals are rounded to half
+    const bool half = mode == PVR_RECORDS_HALF_NORMALS && v->dtype != PVR_F32;
+    const size_t rec_size = half ? sizeof(uint2) : sizeof(float4);
+    PVR_CUDA(vol_alloc((void **)&v->d_records, nrec * rec_size, st));
+    v->records_bytes = nrec * rec_size;
     PVR_CUDA(vol_alloc((void **)&v->d_table, table.size() * sizeof(uint32_t), st));
     PVR_CUDA(vol_alloc((void **)&v->d_bricks, table.size() * sizeof(uint4), st));
     PVR_CUDA(cudaMemcpyAsync(v->d_table, table.data(), table.size() * sizeof(uint32_t),
                              cudaMemcpyHostToDevice, st));
     PVR_CUDA(launch_build_records(v->geo, v->dtype, v->d_vol, v->dims, v->d_nrm, v->normals_mode,
-                                  v->d_table, (float4 *)v->d_records, v->d_bricks, st));
+                                  v->d_table, v->d_records, half, v->d_bricks, st));
     vol_free(v->d_nrm, st);  // given normals now live in the records
     v->d_nrm = nullptr;
-    v->compact = false;
+    v->compact = half;
+    // exact when there are no normals, or when they were computed in half
+    // precision (numpy's arithmetic for float16 input)
+    v->compact_exact = !half || v->normals_mode == PVR_NORMALS_NONE ||
+                       (v->dtype == PVR_F16 && v->normals_mode == PVR_NORMALS_DEVICE);
     PVR_CUDA(cudaStreamSynchronize(st));  // `table` leaves scope; ready for any stream
     v->layout_ready = true;
-    if (g_compact_records.load()) try_compact_records(v, st);
+    if (mode == PVR_RECORDS_HALF_EXACT) try_compact_records(v, st, false);
     return PVR_OK;
 }
 
 // Half records when every value and normal is a half exactly: float16
 // volumes with normals computed in half precision (numpy's arithmetic for
 // float16 input) always are, uint8 values are too.  The march reads half as
-// many bytes per sample and decodes the same floats.  The float records stay
-// when some float is not a half, or when the memory for the copy is missing.
-// Nothing may read the volume meanwhile.  Returns 1 if the records are halves.
-int try_compact_records(pvr_volume *v, cudaStream_t st) {
+// many bytes per sample and decodes the same floats.  round_normals: the
+// values must still be halves exactly, the normal components are rounded to
+// half (relative error <= 2^-11 per component).  The float records stay when
+// a float that must be exact is not a half, or when the memory for the copy
+// is missing.  Nothing may read the volume meanwhile.  Returns 1 if the
+// records are halves.
+int try_compact_records(pvr_volume *v, cudaStream_t st, bool round_normals) {
     if (v->compact) return 1;
     const size_t nrec = v->records_bytes / sizeof(float4);
     uint2 *compact = nullptr;
@@ -174,11 +191,13 @@ int try_compact_records(pvr_volume *v, cudaStream_t st) {
     cudaGetLastError();  // a failed allocation or launch above only means: keep the float records
     cudaStreamSynchronize(st);
     vol_free(d_flag, st);
-    if (compact && inexact == 0) {
+    const int forbidden = round_normals ? 1 : 3;  // inexact values (bit 0), normals (bit 1)
+    if (compact && (inexact & forbidden) == 0) {
         vol_free(v->d_records, st);
         v->d_records = compact;
         v->records_bytes = nrec * sizeof(uint2);
         v->compact = true;
+        v->compact_exact = inexact == 0;
     } else {
         vol_free(compact, st);
     }
@@ -188,7 +207,7 @@ int try_compact_records(pvr_volume *v, cudaStream_t st) {
 
 // Validated job -> the descriptor the kernel reads (everything the fragment
 // shader derives per fragment but that is constant over the frame).
-int fill_job(const pvr_job &j, int tile_w, int tile_h, JobDesc &out) {
+int fill_job(const pvr_job &j, int tile_w, int tile_h, bool fast, JobDesc &out) {
     std::memset(&out, 0, sizeof(out));
     if (!j.volume || !j.lut) return fail(PVR_ERR_VALUE, "job without volume or LUT");
     if (!j.volume->layout_ready) return fail(PVR_ERR_STATE, "volume layout not built");
@@ -225,6 +244,9 @@ int fill_job(const pvr_job &j, int tile_w, int tile_h, JobDesc &out) {
     f.value_scale = v.value_scale;
     f.lut_size = j.lut->size;
     f.flut_size = (float)j.lut->size;
+    f.flut_max = (float)(j.lut->size - 1);
+    f.alpha_k2 = (float)((double)f.alpha_k * 1.4426950408889634);  // * log2(e)
+    out.fast = fast ? 1 : 0;
     out.records = v.d_records;
     out.compact = v.compact ? 1 : 0;
     out.bricks = v.d_bricks;
@@ -314,6 +336,12 @@ int pvr_volume_create(const void *data, int dtype, int d, int h, int w, float va
         if (e != cudaSuccess) return bail(pvr::cuda_fail(e, "upload normals"));
     }
     if (int rc = pvr::ensure_volume_layout(v, st)) return bail(rc);
+    // the records hold every stored value: the uploaded voxels are not needed
+    // again (a volume resource is never laid out twice)
+    pvr::vol_free(v->d_vol, st);
+    v->d_vol = nullptr;
+    v->vol_bytes = 0;
+    cudaStreamSynchronize(st);
     cudaStreamDestroy(st);
     *out = v;
     return PVR_OK;
@@ -335,8 +363,29 @@ int pvr_volume_release(pvr_volume *v, void *stream) {
     return PVR_OK;
 }
 
-int pvr_set_compact_records(int enabled) {
-    pvr::g_compact_records.store(enabled ? 1 : 0);
+int pvr_set_compact_records(int mode) {
+    if (mode < PVR_RECORDS_FLOAT || mode > PVR_RECORDS_HALF_NORMALS)
+        return fail(PVR_ERR_VALUE, "record mode must be 0 (float), 1 (half where exact) or 2 (half normals)");
+    pvr::g_compact_records.store(mode);
+    return PVR_OK;
+}
+
+int pvr_get_compact_records(int *mode) {
+    if (!mode) return fail(PVR_ERR_VALUE, "NULL argument");
+    *mode = pvr::g_compact_records.load();
+    return PVR_OK;
+}
+
+int pvr_set_arithmetic(int mode) {
+    if (mode != PVR_ARITH_FAST && mode != PVR_ARITH_EXACT)
+        return fail(PVR_ERR_VALUE, "arithmetic must be 0 (fast) or 1 (exact)");
+    pvr::g_arithmetic.store(mode);
+    return PVR_OK;
+}
+
+int pvr_get_arithmetic(int *mode) {
+    if (!mode) return fail(PVR_ERR_VALUE, "NULL argument");
+    *mode = pvr::g_arithmetic.load();
     return PVR_OK;
 }
 
@@ -359,7 +408,7 @@ int pvr_volume_compact(pvr_volume *v, int *compacted) {
         if (dev != v->device) cudaSetDevice(dev);
         return pvr::cuda_fail(e, "cudaStreamCreateWithFlags");
     }
-    const int c = pvr::try_compact_records(v, st);
+    const int c = pvr::try_compact_records(v, st, false);
     cudaStreamDestroy(st);
     if (dev != v->device) cudaSetDevice(dev);
     if (compacted) *compacted = c;
@@ -370,6 +419,13 @@ int pvr_volume_record_bytes(const pvr_volume *v, int *bytes) {
     if (!v || !bytes) return fail(PVR_ERR_VALUE, "NULL argument");
     if (!v->layout_ready) return fail(PVR_ERR_STATE, "volume layout not built");
     *bytes = v->compact ? (int)sizeof(uint2) : (int)sizeof(float4);
+    return PVR_OK;
+}
+
+int pvr_volume_records_exact(const pvr_volume *v, int *exact) {
+    if (!v || !exact) return fail(PVR_ERR_VALUE, "NULL argument");
+    if (!v->layout_ready) return fail(PVR_ERR_STATE, "volume layout not built");
+    *exact = (!v->compact || v->compact_exact) ? 1 : 0;
     return PVR_OK;
 }
 

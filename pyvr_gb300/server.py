@@ -32,6 +32,7 @@ from __future__ import annotations
 import collections
 import ctypes
 import gc
+import heapq
 import queue
 import threading
 import time
@@ -64,6 +65,9 @@ class RenderRequest:
     height: int
     value_scale: float = 1.0
     volume: object = None
+    # > 0: the request fails with TimeoutError if its image is not back this
+    # many seconds after its arrival (native server)
+    timeout_s: float = 0.0
     arrival: float = 0.0
     tag: str = ""
     future: Future = field(default_factory=Future)
@@ -72,12 +76,23 @@ class RenderRequest:
 
 
 class VolumeCache:
-    """HBM-resident volumes with a byte budget and LRU eviction."""
+    """HBM-resident volumes with a byte budget and LRU eviction.
 
-    def __init__(self, budget_bytes: int, brick_log2: int = 3, half_records: bool = False):
+    Failure handling: when every resident volume is pinned by in-flight
+    requests, a new volume is admitted over budget rather than stalling the
+    request stream (counted in ``over_budget``); when a layout fails for lack
+    of device memory (``MemoryError``), unpinned volumes are evicted, least
+    recently used first, and the layout is retried (counted in
+    ``alloc_retries``) until it succeeds or nothing is left to evict."""
+
+    def __init__(self, budget_bytes: int, brick_log2: int = 3, half_records: bool = False,
+                 release_wait=None):
         self.budget = int(budget_bytes)
         self.brick_log2 = brick_log2
         self.half_records = half_records
+        # release_wait(): wait until the memory of volumes released so far is
+        # free again (before retrying a failed layout)
+        self.release_wait = release_wait
         self._vols: "collections.OrderedDict[int, DeviceVolume]" = collections.OrderedDict()
         self._bytes: Dict[int, int] = {}
         self._users: Dict[int, int] = collections.defaultdict(int)  # in-flight batches
@@ -85,6 +100,24 @@ class VolumeCache:
         self.evictions = 0
         self.loads = 0
         self.uploaded_bytes = 0  # host bytes of the volumes uploaded so far
+        self.over_budget = 0     # admissions past the budget (every resident volume pinned)
+        self.alloc_retries = 0   # layouts retried after evicting on a failed allocation
+
+    def estimate_bytes(self, volume) -> int:
+        """Device bytes a layout of ``volume`` needs at its peak: the records
+        (8-byte halves for uint8 / float16 volumes when the library lays them
+        out that way, else 16-byte floats) plus the uploaded voxels."""
+        d, h, w = volume.data.shape
+        rec = 16
+        if np.asarray(volume.data).dtype in (np.uint8, np.float16):
+            from .batch import get_compact_records
+            try:
+                rec = 8 if get_compact_records() == "half_normals" else 16
+            except Exception:
+                rec = 16
+        lb = self.brick_log2
+        return int(rec * ((w >> lb) + 1) * ((h >> lb) + 1) * ((d >> lb) + 1) * ((1 << lb) + 1) ** 3
+                   + volume.data.nbytes)
 
     @property
     def used(self) -> int:
@@ -120,15 +153,22 @@ class VolumeCache:
         for dv in vols:
             dv.close()
 
+    def _evict_one(self, release_after) -> bool:
+        """Evict the least recently used unpinned volume; False if none."""
+        victim = next((k for k in self._vols if self._users.get(k, 0) == 0), None)
+        if victim is None:
+            return False
+        dv = self._vols.pop(victim)
+        self._bytes.pop(victim)
+        release_after(dv)
+        self.evictions += 1
+        return True
+
     def _evict_for(self, need: int, release_after) -> None:
         while self.used + need > self.budget:
-            victim = next((k for k in self._vols if self._users.get(k, 0) == 0), None)
-            if victim is None:
-                break  # everything is in use: go over budget rather than stall
-            dv = self._vols.pop(victim)
-            self._bytes.pop(victim)
-            release_after(dv)
-            self.evictions += 1
+            if not self._evict_one(release_after):
+                self.over_budget += 1  # everything is in use: go over budget rather than stall
+                return
 
     def insert(self, vid: int, volume, value_scale: float, release_after) -> DeviceVolume:
         """Upload + lay out (device normals) a volume and make it resident
@@ -137,15 +177,25 @@ class VolumeCache:
             if vid in self._vols:
                 self._vols.move_to_end(vid)
                 return self._vols[vid]
-        d, h, w = volume.data.shape
-        est = int(16 * ((w >> self.brick_log2) + 1) * ((h >> self.brick_log2) + 1) *
-                  ((d >> self.brick_log2) + 1) * ((1 << self.brick_log2) + 1) ** 3
-                  + volume.data.nbytes)
+        est = self.estimate_bytes(volume)
         with self._lock:
             self._evict_for(est, release_after)
         normals = "given" if getattr(volume, "normals", None) is not None else "device"
-        dv = DeviceVolume(volume, value_scale=value_scale, normals=normals,
-                          brick_log2=self.brick_log2, half_records=self.half_records)
+        while True:
+            try:
+                dv = DeviceVolume(volume, value_scale=value_scale, normals=normals,
+                                  brick_log2=self.brick_log2, half_records=self.half_records)
+                break
+            except MemoryError:
+                # the device is fuller than the budget assumed (other memory
+                # users, fragmentation): make room and try again
+                with self._lock:
+                    evicted = self._evict_one(release_after)
+                if not evicted:
+                    raise
+                self.alloc_retries += 1
+                if self.release_wait is not None:
+                    self.release_wait()
         with self._lock:
             if vid in self._vols:  # loaded meanwhile by another request
                 release_after(dv)
@@ -155,6 +205,29 @@ class VolumeCache:
             self.loads += 1
             self.uploaded_bytes += int(volume.data.nbytes)
         return dv
+
+
+class Deadlines:
+    """Request deadlines by tag: ``expired(now)`` pops the tags whose
+    deadline has passed, earliest first."""
+
+    def __init__(self):
+        self._heap: List[tuple] = []
+        self._lock = threading.Lock()
+
+    def add(self, tag, when: float) -> None:
+        with self._lock:
+            heapq.heappush(self._heap, (when, tag))
+
+    def expired(self, now: float) -> list:
+        out = []
+        with self._lock:
+            while self._heap and self._heap[0][0] <= now:
+                out.append(heapq.heappop(self._heap)[1])
+        return out
+
+    def __len__(self) -> int:
+        return len(self._heap)
 
 
 def tf_key(color_tf, opacity_tf) -> tuple:
@@ -631,12 +704,15 @@ class NativeRenderServer:
                  batch_pixels: int = 512 * 512, lut_reserve: int = 1024, half_records: bool = False):
         import torch
         self.torch = torch
-        self.cache = VolumeCache(budget_bytes, brick_log2, half_records)
+        self._release_stream = torch.cuda.Stream()
+        self.cache = VolumeCache(budget_bytes, brick_log2, half_records,
+                                 release_wait=self._release_stream.synchronize)
         self.luts = LutCache()
         self.luts.reserve(256, lut_reserve)
         self.per_frame = per_frame
+        self._deadlines = Deadlines()
+        self.timeouts = 0
         self._lut_stream = torch.cuda.Stream()
-        self._release_stream = torch.cuda.Stream()
         self._lock = threading.Lock()  # LUT cache and in-flight table
         self._pool = _PinnedPool(torch)
         self._lib = _native.load()
@@ -659,10 +735,17 @@ class NativeRenderServer:
 
     # -- client API -------------------------------------------------------------
     def submit(self, req: RenderRequest) -> Future:
+        """Queue a request; its future gets the image (or the exception).  In
+        the per-frame baseline a new-volume load runs here, in the caller's
+        thread, before the request's render is queued: a serial renderer
+        serves the load before anything that arrives after it."""
         if not req.arrival:
             req.arrival = time.perf_counter()
         if req.kind == "load":
-            self._loads.put(req)
+            if self.per_frame:
+                self._load_then_render(req)
+            else:
+                self._loads.put(req)
         else:
             self._submit_render(req)
         return req.future
@@ -704,19 +787,26 @@ class NativeRenderServer:
         _native.check(self._lib.pvr_volume_release(dv.handle, self._release_stream.cuda_stream))
         dv.handle = None
 
+    def _load_then_render(self, req: RenderRequest) -> None:
+        if req.timeout_s > 0 and time.perf_counter() > req.arrival + req.timeout_s:
+            self.timeouts += 1
+            req.future.set_exception(TimeoutError(f"request timed out after {req.timeout_s} s before its load"))
+            return
+        try:
+            self.cache.insert(req.volume_id, req.volume, req.value_scale, self._free_volume)
+        except Exception as e:
+            req.future.set_exception(e)
+            return
+        req.kind = "render"
+        self._submit_render(req)
+
     def _load_loop(self) -> None:
         self.torch.cuda.set_device(self.torch.cuda.current_device())
         while True:
             req = self._loads.get()
             if req is None or self._stop:
                 return
-            try:
-                self.cache.insert(req.volume_id, req.volume, req.value_scale, self._free_volume)
-            except Exception as e:
-                req.future.set_exception(e)
-                continue
-            req.kind = "render"
-            self._submit_render(req)
+            self._load_then_render(req)
 
     def _submit_render(self, req: RenderRequest) -> None:
         dv = self.cache.acquire(req.volume_id)
@@ -762,6 +852,8 @@ class NativeRenderServer:
             r.out_pinned = int(slab is not None)
             r.tag = tag
             self._inflight[tag] = (req, req.volume_id, key, out)
+            if req.timeout_s > 0:
+                self._deadlines.add(tag, req.arrival + req.timeout_s)
             rc = self._lib.pvr_server_submit(self._h, ctypes.byref(r))
             if rc == _native.PVR_ERR_VALUE and b"parallel" in self._lib.pvr_last_error():
                 # degenerate orbit camera: the Camera methods' matrices
@@ -797,6 +889,10 @@ class NativeRenderServer:
                     self.luts.release(key)
                 req.done_at = c.t_done_ns / 1e9
                 req.launched_at = c.t_launch_ns / 1e9
+                if req.future.done():  # failed by its deadline: the image is dropped
+                    if not isinstance(out, np.ndarray):
+                        self._pool.put(*out)
+                    continue
                 if not isinstance(out, np.ndarray):
                     if c.status == 0:
                         out = self._pool.wrap(*out)
@@ -808,6 +904,15 @@ class NativeRenderServer:
                     req.future.set_exception(RuntimeError(
                         f"render failed (status {c.status}): "
                         f"{self._lib.pvr_server_last_error(self._h).decode(errors='replace')}"))
+            if len(self._deadlines):
+                # requests past their deadline fail now; their launches still
+                # finish (their memory stays in use until then)
+                for tag in self._deadlines.expired(time.perf_counter()):
+                    entry = self._inflight.get(tag)
+                    if entry is not None and not entry[0].future.done():
+                        self.timeouts += 1
+                        entry[0].future.set_exception(
+                            TimeoutError(f"request timed out after {entry[0].timeout_s} s"))
             if self._stop and not self._inflight:
                 return
 

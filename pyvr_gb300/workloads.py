@@ -186,11 +186,13 @@ def config_batching(n: int = 64, max_dim: int = 384, resolutions=(128, 256, 512,
 # Serving workload
 # ---------------------------------------------------------------------------
 
-def value_noise_device(n, seed: int) -> np.ndarray:
+def value_noise_device(n, seed: int, dtype: str = "f32") -> np.ndarray:
     """value_noise(shape, seed) (shape = n or (n, n, n)) by the same definition
     (lattices from default_rng(seed), align-corners trilinear upsampling,
     weights 0.5^k, min-max normalisation), upsampled on the GPU for speed;
-    float rounding may differ from value_noise in the last bits."""
+    float rounding may differ from value_noise in the last bits.  dtype: the
+    storage of the result ("f32", or "u8" / "f16" as ``to_storage`` makes
+    them, converted on the GPU)."""
     import torch
     import torch.nn.functional as F
     shape = (n, n, n) if isinstance(n, (int, np.integer)) else tuple(int(x) for x in n)
@@ -200,8 +202,57 @@ def value_noise_device(n, seed: int) -> np.ndarray:
         v = torch.from_numpy(rng.random((lat, lat, lat), dtype=np.float32)).cuda()
         up = F.interpolate(v[None, None], size=shape, mode="trilinear", align_corners=True)[0, 0]
         acc += (0.5 ** k) * up
+        del up
     lo, hi = acc.min(), acc.max()
-    return ((acc - lo) / (hi - lo)).cpu().numpy()
+    acc = (acc - lo) / (hi - lo)
+    if dtype == "u8":
+        # round half to even, as numpy's rint
+        return torch.round(acc * 255.0).to(torch.uint8).cpu().numpy()
+    if dtype == "f16":
+        return acc.to(torch.float16).cpu().numpy()
+    return acc.cpu().numpy()
+
+
+class _LazyVolumes:
+    """The workload's volumes as (Volume, value_scale), generated on first
+    use (``materialize`` generates them all)."""
+
+    def __init__(self, specs, generator):
+        self._specs = specs  # (extent, storage, seed)
+        self._gen = generator
+        self._cache = {}
+
+    def __len__(self):
+        return len(self._specs)
+
+    def __getitem__(self, i):
+        if i < 0:
+            i += len(self._specs)
+        if i not in self._cache:
+            n, dtype, seed = self._specs[i]
+            data = self._gen(n, seed, dtype)
+            vol = Volume(data=data, min_bounds=np.array([-1.0, -1.0, -1.0], np.float32),
+                         max_bounds=np.array([1.0, 1.0, 1.0], np.float32))
+            self._cache[i] = (vol, 1.0 / 255.0 if dtype == "u8" else 1.0)
+        return self._cache[i]
+
+    def __iter__(self):
+        return (self[i] for i in range(len(self)))
+
+    def extent(self, i) -> int:
+        return self._specs[i][0]
+
+    def storage(self, i) -> str:
+        return self._specs[i][1]
+
+    def materialize(self) -> None:
+        for i in range(len(self)):
+            self[i]
+
+
+def _storage_generator(gen):
+    """A (n, seed) -> float volume generator as (n, seed, dtype) -> storage."""
+    return lambda n, seed, dtype: to_storage(gen(n, seed), dtype)
 
 
 class ServingWorkload:
@@ -211,26 +262,32 @@ class ServingWorkload:
     request streams with the mix 70% orbit re-renders (azimuth/elevation
     deltas ~N(0, 0.05) rad, 512^2), 20% TF edits (1-3 opacity points moved by
     ~N(0, 0.05), then a 512^2 render), 5% high-quality 1024^2 captures, 5%
-    new-volume loads (a volume not resident, uploaded and laid out, then
-    rendered at 512^2)."""
+    new-volume loads (a volume not in the catalog replaces a catalog slot:
+    uploaded, laid out with device normals, then rendered at 512^2).
+
+    The n_extra volumes outside the catalog are the clients' pool of new
+    volumes; a load brings the one that has been out of the catalog longest,
+    so with a pool larger than what the byte budget holds, every load uploads
+    a volume that is not resident.  Volume data is generated on first use
+    (``volumes.materialize()`` generates it all up front)."""
 
     def __init__(self, n_volumes: int = 32, n_extra: int = 16, min_dim: int = 128,
                  max_dim: int = 512, seed: int = 0, res: int = 512, capture_res: int = 1024,
                  generator=None):
-        gen = generator or value_noise_device
         self.res, self.capture_res = res, capture_res
         self.light = Light.directional([1, -1, 0], 0.2, 0.8)
-        self.volumes = []  # (Volume, value_scale)
         rng = np.random.default_rng(seed)
+        specs = []
         for i in range(n_volumes + n_extra):
             n = int(round(np.exp(rng.uniform(np.log(min_dim), np.log(max_dim)))))
             dtype = "u8" if rng.random() < 0.5 else "f16"
-            data = to_storage(gen(n, 5000 + i), dtype)
-            vol = Volume(data=data, min_bounds=np.array([-1.0, -1.0, -1.0], np.float32),
-                         max_bounds=np.array([1.0, 1.0, 1.0], np.float32))
-            self.volumes.append((vol, 1.0 / 255.0 if dtype == "u8" else 1.0))
+            specs.append((n, dtype, 5000 + i))
+        gen = value_noise_device if generator is None else _storage_generator(generator)
+        self.volumes = _LazyVolumes(specs, gen)
         self.n_catalog = n_volumes
         self.catalog = list(range(n_volumes))  # catalog slot -> volume index
+        # volumes out of the catalog, the longest-out first
+        self.outside = list(range(n_volumes, n_volumes + n_extra))
         self.sessions = []
         for i in range(n_volumes + n_extra):
             srng = np.random.default_rng(9000 + i)
@@ -240,16 +297,17 @@ class ServingWorkload:
                 "otf": [(float(x), float(y)) for x, y in zip(np.sort(srng.random(6)),
                                                             srng.uniform(0.0, 0.3, 6))],
                 "ctf": standin_colormap(int(srng.integers(0, N_STANDIN_COLORMAPS)))})
-        self._next_extra = n_volumes
 
     def snapshot(self):
-        """The evolving state (catalog, session cameras and opacity points), to
-        restart request streams from the same point with ``restore``."""
-        return (list(self.catalog), [dict(s, otf=list(s["otf"])) for s in self.sessions])
+        """The evolving state (catalog, volumes outside it, session cameras and
+        opacity points), to restart request streams from the same point with
+        ``restore``."""
+        return (list(self.catalog), list(self.outside), [dict(s, otf=list(s["otf"])) for s in self.sessions])
 
     def restore(self, snap) -> None:
-        catalog, sessions = snap
+        catalog, outside, sessions = snap
         self.catalog = list(catalog)
+        self.outside = list(outside)
         self.sessions = [dict(s, otf=list(s["otf"])) for s in sessions]
 
     def camera(self, vidx: int) -> Camera:
@@ -276,9 +334,10 @@ class ServingWorkload:
                 tag, w, cfg = "capture", self.capture_res, RenderConfig.high_quality()
             else:
                 tag, kind = "load", "load"
-                # a volume that is not in the catalog replaces a catalog slot
-                out_of_catalog = [i for i in range(len(self.volumes)) if i not in self.catalog]
-                self.catalog[slot] = out_of_catalog[int(rng.integers(0, len(out_of_catalog)))]
+                # the volume out of the catalog longest replaces a catalog slot
+                if self.outside:
+                    self.outside.append(self.catalog[slot])
+                    self.catalog[slot] = self.outside.pop(0)
             vidx = self.catalog[slot]
             s = self.sessions[vidx]
             if tag == "orbit":

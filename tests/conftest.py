@@ -24,3 +24,16 @@ def gpu_available() -> bool:
 def native_lib():
     from pyvr_gb300 import _native
     return _native.load()
+
+
+@pytest.fixture(scope="session", autouse=True)
+def exact_arithmetic():
+    """The GPU tests compare renders with the oracle bit for bit, so they run
+    the exact arithmetic; tests of the fast arithmetic (the library's default)
+    switch to it with ``pyvr_gb300.batch.arithmetic("fast")``."""
+    try:
+        from pyvr_gb300.batch import set_arithmetic
+        set_arithmetic("exact")
+    except Exception:  # no library (CPU-only checks that do not need it)
+        pass
+    yield

@@ -23,19 +23,44 @@ def nan_equal(a, b):
     return a.shape == b.shape and bool(np.all((a == b) | (np.isnan(a) & np.isnan(b))))
 
 
+@pytest.mark.parametrize("dims,brick_log2", [((13, 17, 22), 3), ((33, 33, 33), 3), ((16, 16, 16), 4),
+                                              ((2, 2, 2), 2), ((21, 21, 21), 2), ((40, 40, 40), 4)])
 @pytest.mark.parametrize("dtype", ["u8", "f16", "f32"])
-def test_device_normals_match_numpy(dtype):
-    rng = np.random.default_rng(41)
-    base = W.value_noise((13, 17, 22), seed=3)
+def test_device_normals_match_numpy(dtype, dims, brick_log2):
+    # cubic volumes take the normals from the neighbours staged in shared
+    # memory, non-cubic ones from global memory; both must equal numpy
+    base = W.value_noise(dims, seed=3)
     data = W.to_storage(base, dtype)
-    data[2:5, 3:6, :] = data[3, 4, 0]  # flat patches: zero gradients (NaN for float16)
+    if min(dims) > 6:
+        data[2:5, 3:6, :] = data[3, 4, 0]  # flat patches: zero gradients (NaN for float16)
     vol = Volume(data=data)
-    dv = DeviceVolume(vol, normals="device")
+    dv = DeviceVolume(vol, normals="device", brick_log2=brick_log2)
     got = dv.read_normals()
     want = compute_normal_volume(data)
     assert nan_equal(got, want), np.nanmax(np.abs(got - want))
-    if dtype == "f16":
+    if dtype == "f16" and min(dims) > 6:
         assert np.isnan(want).any()  # the reference's own float16 behaviour
+
+
+@pytest.mark.parametrize("dtype", ["u8", "f16", "f32"])
+def test_half_normal_records(dtype):
+    # "half_normals": uint8 / float16 volumes get 8-byte records holding the
+    # values exactly and the normals rounded to half; float32 keeps floats
+    from pyvr_gb300.batch import set_compact_records
+    data = W.to_storage(W.value_noise((24, 24, 24), seed=5), dtype)
+    set_compact_records("half_normals")
+    try:
+        dv = DeviceVolume(Volume(data=data), normals="device", brick_log2=3)
+    finally:
+        set_compact_records("float")
+    want = compute_normal_volume(data)
+    if dtype == "f32":
+        assert dv.record_bytes() == 16 and dv.records_exact()
+        assert nan_equal(dv.read_normals(), want)
+    else:
+        assert dv.record_bytes() == 8
+        assert dv.records_exact() == (dtype == "f16")
+        assert nan_equal(dv.read_normals(), want.astype(np.float16).astype(np.float32))
 
 
 def test_given_normals_roundtrip():

@@ -34,14 +34,32 @@ def test_camera_matches_reference(i):
 
 @pytest.mark.parametrize("i", range(len(G["camera_params"])))
 def test_batch_camera_setup_matches_reference(i, native_lib):
-    # the batch path's native double-precision camera setup: the reference's
-    # float32 matrices to float32 rounding
+    # the batch path's native camera setup takes the reference's float32
+    # steps in float32: its float32 matrices equal the reference's as the
+    # Camera methods' do (up to the last bit of entries that are ~0)
     from pyvr_gb300.batch import job_camera_uniforms
     p = G["camera_params"][i]
     view, proj, pos = job_camera_uniforms(_camera(p), float(p[8]), 1.0)
-    np.testing.assert_allclose(pos, G["camera_pos"][i], rtol=0, atol=2e-6)
-    np.testing.assert_allclose(view, G["camera_view"][i], rtol=0, atol=2e-6)
+    np.testing.assert_allclose(pos, G["camera_pos"][i].astype(np.float32), rtol=0, atol=0)
+    np.testing.assert_allclose(view, G["camera_view"][i], rtol=2e-7, atol=1e-12)
     np.testing.assert_allclose(proj, G["camera_proj"][i], rtol=2e-7, atol=0)
+
+
+def test_batch_camera_setup_equals_camera_methods(native_lib):
+    # 4000 orbit cameras: the native setup and Camera.get_view_matrix /
+    # get_projection_matrix / get_camera_vectors give the same float32 arrays,
+    # every entry bit for bit except the ones that are rounding noise of 0
+    from pyvr_gb300.batch import job_camera_uniforms
+    from pyvr_gb300.renderer import camera_uniforms
+    rng = np.random.default_rng(11)
+    for k in range(4000):
+        cam = Camera.from_spherical(np.zeros(3, np.float32), float(rng.uniform(-4, 4)),
+                                    float(rng.uniform(-1.5, 1.5)), float(rng.uniform(-0.5, 0.5)) if k % 2 else 0.0,
+                                    float(rng.uniform(2.0, 5.0)))
+        w, h = [(512, 512), (1024, 768), (37, 91)][k % 3]
+        for a, b in zip(job_camera_uniforms(cam, w, h), camera_uniforms(cam, w, h)):
+            differ = a != b
+            assert np.all(np.abs(a[differ]) < 1e-12) and np.all(np.abs(b[differ]) < 1e-12), (k, a, b)
 
 
 def test_batch_camera_setup_rejects_bad_cameras(native_lib):

@@ -172,3 +172,27 @@ def test_native_server_with_evictions_and_bad_requests():
     with pytest.raises(KeyError):
         server.submit(RenderRequest(**kw)).result(timeout=30)
     server.close()
+
+
+def test_native_server_request_deadline():
+    """A request whose image is not back within its timeout fails with
+    TimeoutError (launches held by pause()); its launch still completes and
+    the server keeps serving: a later request returns the same image as a
+    request without a deadline."""
+    from pyvr_gb300.server import NativeRenderServer
+    wl = _workload()
+    stream = wl.requests(rate=4000.0, duration=0.2, seed=5)
+    server = NativeRenderServer(budget_bytes=1 << 30, max_batch=4, slots=2)
+    vol, vs = wl.volumes[0]
+    server.cache.insert(0, vol, vs, server._free_volume)
+    base = dict(stream[0][1], volume_id=0, kind="render")
+    server.pause(True)
+    late = RenderRequest(**dict(base, timeout_s=0.05))
+    fut = server.submit(late)
+    with pytest.raises(TimeoutError):
+        fut.result(timeout=10)
+    server.pause(False)
+    a = server.submit(RenderRequest(**base)).result(timeout=30)
+    b = server.submit(RenderRequest(**dict(base, timeout_s=10.0))).result(timeout=30)
+    assert a.tobytes() == b.tobytes() and server.timeouts == 1
+    server.close()

@@ -77,15 +77,76 @@ def test_volume_cache_budget_lru_and_pins(fake_device):
     cache.insert(3, _vol(16), 1.0, released.append)
     assert cache.get(2) is None and cache.get(1) is not None and cache.get(3) is not None
     assert len(released) == 1 and cache.evictions >= 1
-    # everything pinned: go over budget rather than stall
+    # everything pinned: go over budget rather than stall, and count it
     cache.acquire(3)
+    assert cache.over_budget == 0
     cache.insert(4, _vol(16), 1.0, released.append)
     assert cache.get(1) is not None and cache.get(3) is not None and cache.get(4) is not None
+    assert cache.over_budget == 1 and cache.used > cache.budget
     cache.release(1)
     cache.release(3)
     vols = [cache.get(i) for i in (1, 3, 4)]
     cache.clear()
     assert all(v.closed for v in vols) and cache.used == 0
+
+
+def test_volume_cache_evicts_and_retries_when_allocation_fails(fake_device, monkeypatch):
+    """A layout that runs out of device memory (the budget assumed more room
+    than there is) evicts the least recently used unpinned volume and is
+    retried; with nothing left to evict the MemoryError reaches the caller."""
+    one = FakeDeviceVolume(_vol(16), brick_log2=3).device_bytes()
+    FakeDeviceVolume.made = []
+    failures = {"left": 2}
+
+    class Flaky(FakeDeviceVolume):
+        def __init__(self, *a, **kw):
+            if failures["left"] > 0:
+                failures["left"] -= 1
+                raise MemoryError("out of device memory (injected)")
+            super().__init__(*a, **kw)
+
+    monkeypatch.setattr(S, "DeviceVolume", FakeDeviceVolume)
+    waits = []
+    cache = S.VolumeCache(budget_bytes=one * 10, brick_log2=3, release_wait=lambda: waits.append(1))
+    released = []
+    for vid in (1, 2, 3):
+        cache.insert(vid, _vol(16), 1.0, released.append)
+    cache.acquire(3)  # pinned: never a victim
+    monkeypatch.setattr(S, "DeviceVolume", Flaky)
+    cache.insert(4, _vol(16), 1.0, released.append)
+    # two failed attempts: volumes 1 then 2 (least recent first) were evicted
+    assert cache.alloc_retries == 2 and len(waits) == 2
+    assert cache.get(1) is None and cache.get(2) is None
+    assert cache.get(3) is not None and cache.get(4) is not None
+    assert cache.evictions == 2 and len(released) == 2
+    # nothing evictable left (3 and 4 pinned): the failure propagates
+    cache.acquire(4)
+    failures["left"] = 5
+    with pytest.raises(MemoryError):
+        cache.insert(5, _vol(16), 1.0, released.append)
+    assert cache.get(5) is None and cache.alloc_retries == 2
+
+
+def test_volume_cache_estimate_follows_record_form(monkeypatch):
+    import pyvr_gb300.batch as B
+    cache = S.VolumeCache(budget_bytes=1 << 40, brick_log2=4)
+    vol8 = Volume(data=np.zeros((32, 32, 32), np.uint8))
+    vol32 = Volume(data=np.zeros((32, 32, 32), np.float32))
+    records = 3 ** 3 * 17 ** 3
+    monkeypatch.setattr(B, "get_compact_records", lambda: "half_normals")
+    assert cache.estimate_bytes(vol8) == 8 * records + 32 ** 3
+    assert cache.estimate_bytes(vol32) == 16 * records + 4 * 32 ** 3
+    monkeypatch.setattr(B, "get_compact_records", lambda: "float")
+    assert cache.estimate_bytes(vol8) == 16 * records + 32 ** 3
+
+
+def test_deadlines_expire_in_order():
+    d = S.Deadlines()
+    for tag, when in ((1, 5.0), (2, 1.0), (3, 3.0)):
+        d.add(tag, when)
+    assert d.expired(0.5) == [] and len(d) == 3
+    assert d.expired(3.0) == [2, 3]
+    assert d.expired(10.0) == [1] and len(d) == 0
 
 
 def _tfs(seed):
