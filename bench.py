@@ -1082,8 +1082,8 @@ def run_reference(args):
     if rank != 0:
         return
     from pyvr_gb300 import workloads as W
-    wl = W.ServingWorkload(n_volumes=args.serving_volumes, n_extra=args.serving_extra, min_dim=128,
-                           max_dim=args.serving_max_dim, seed=0,
+    wl = W.ServingWorkload(n_volumes=args.serving_volumes, n_extra=args.serving_extra,
+                           min_dim=args.serving_min_dim, max_dim=args.serving_max_dim, seed=0,
                            generator=lambda n, s: W.value_noise((n, n, n), s))
     per_step = max(1.0, args.cpu_seconds / max(1, args.steps))
     server = ReferenceServer()

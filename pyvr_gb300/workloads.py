@@ -239,6 +239,13 @@ class _LazyVolumes:
     def __iter__(self):
         return (self[i] for i in range(len(self)))
 
+    def ref(self, i) -> "_VolumeRef":
+        """A stand-in for volume i that generates it on first use."""
+        return _VolumeRef(self, i)
+
+    def value_scale(self, i) -> float:
+        return 1.0 / 255.0 if self._specs[i][1] == "u8" else 1.0
+
     def extent(self, i) -> int:
         return self._specs[i][0]
 
@@ -248,6 +255,22 @@ class _LazyVolumes:
     def materialize(self) -> None:
         for i in range(len(self)):
             self[i]
+
+
+class _VolumeRef:
+    """Volume i of a _LazyVolumes: the Volume's attributes, generated on first
+    access (a request stream can name volumes it never makes anyone read)."""
+
+    def __init__(self, volumes, i):
+        self._volumes, self._i = volumes, i
+
+    def resolve(self) -> Volume:
+        return self._volumes[self._i][0]
+
+    data = property(lambda self: self.resolve().data)
+    normals = property(lambda self: self.resolve().normals)
+    min_bounds = property(lambda self: self.resolve().min_bounds)
+    max_bounds = property(lambda self: self.resolve().max_bounds)
 
 
 def _storage_generator(gen):
@@ -350,8 +373,8 @@ class ServingWorkload:
                     pts[k] = (float(np.clip(x + rng.normal(0, 0.05), 0, 1)),
                               float(np.clip(y + rng.normal(0, 0.05), 0, 1)))
                 s["otf"] = sorted(pts)
-            vol, vs = self.volumes[vidx]
             out.append((t, dict(kind=kind, volume_id=vidx, camera=self.camera(vidx), light=self.light,
                                 config=cfg, color_tf=s["ctf"],
                                 opacity_tf=OpacityTransferFunction(list(s["otf"])), width=w, height=w,
-                                value_scale=vs, volume=vol, tag=tag)))
+                                value_scale=self.volumes.value_scale(vidx), volume=self.volumes.ref(vidx),
+                                tag=tag)))
