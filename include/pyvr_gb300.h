@@ -175,6 +175,12 @@ int pvr_volume_destroy(pvr_volume *v);   /* waits for the whole device first */
  * invalid on return. */
 int pvr_volume_release(pvr_volume *v, void *stream);
 int pvr_volume_device_bytes(const pvr_volume *v, long long *bytes);
+/* Grow the memory pool that volume resources are allocated from (the
+ * current device's stream-ordered pool, which keeps what is freed) to at
+ * least `bytes`, so that volumes created and released later (a serving cache
+ * under a byte budget) take their memory from the pool instead of mapping
+ * new memory while renders run.  No reference counterpart. */
+int pvr_reserve_volume_memory(long long bytes);
 /* Bytes per texel record of the volume's layout: 16 (float value + float
  * normal) or 8 (the same four floats as halves, used when every one of them
  * is a half exactly -- float16 volumes with normals computed in half

@@ -363,6 +363,21 @@ int pvr_volume_release(pvr_volume *v, void *stream) {
     return PVR_OK;
 }
 
+int pvr_reserve_volume_memory(long long bytes) {
+    if (bytes < 0) return fail(PVR_ERR_VALUE, "bytes must be >= 0");
+    if (bytes == 0) return PVR_OK;
+    cudaStream_t st = nullptr;
+    PVR_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    void *p = nullptr;
+    cudaError_t e = pvr::vol_alloc(&p, (size_t)bytes, st);
+    if (e == cudaSuccess) cudaFreeAsync(p, st);
+    cudaError_t e2 = cudaStreamSynchronize(st);
+    cudaStreamDestroy(st);
+    if (e != cudaSuccess) return pvr::cuda_fail(e, "reserve volume memory");
+    if (e2 != cudaSuccess) return pvr::cuda_fail(e2, "reserve volume memory");
+    return PVR_OK;
+}
+
 int pvr_set_compact_records(int mode) {
     if (mode < PVR_RECORDS_FLOAT || mode > PVR_RECORDS_HALF_NORMALS)
         return fail(PVR_ERR_VALUE, "record mode must be 0 (float), 1 (half where exact) or 2 (half normals)");

@@ -153,33 +153,41 @@ class VolumeCache:
         for dv in vols:
             dv.close()
 
-    def _evict_one(self, release_after) -> bool:
-        """Evict the least recently used unpinned volume; False if none."""
+    def _evict_one(self):
+        """Take the least recently used unpinned volume out of the cache (the
+        caller releases its memory, outside the lock); None if none."""
         victim = next((k for k in self._vols if self._users.get(k, 0) == 0), None)
         if victim is None:
-            return False
+            return None
         dv = self._vols.pop(victim)
         self._bytes.pop(victim)
-        release_after(dv)
         self.evictions += 1
-        return True
+        return dv
 
-    def _evict_for(self, need: int, release_after) -> None:
+    def _evict_for(self, need: int) -> list:
+        out = []
         while self.used + need > self.budget:
-            if not self._evict_one(release_after):
+            dv = self._evict_one()
+            if dv is None:
                 self.over_budget += 1  # everything is in use: go over budget rather than stall
-                return
+                break
+            out.append(dv)
+        return out
 
     def insert(self, vid: int, volume, value_scale: float, release_after) -> DeviceVolume:
         """Upload + lay out (device normals) a volume and make it resident
-        (a volume that is already resident is kept as it is)."""
+        (a volume that is already resident is kept as it is).  Evicted
+        volumes are handed to ``release_after`` outside the cache's lock, so
+        that no device call holds up the requests that look volumes up."""
         with self._lock:
             if vid in self._vols:
                 self._vols.move_to_end(vid)
                 return self._vols[vid]
         est = self.estimate_bytes(volume)
         with self._lock:
-            self._evict_for(est, release_after)
+            evicted = self._evict_for(est)
+        for dv in evicted:
+            release_after(dv)
         normals = "given" if getattr(volume, "normals", None) is not None else "device"
         while True:
             try:
@@ -190,20 +198,23 @@ class VolumeCache:
                 # the device is fuller than the budget assumed (other memory
                 # users, fragmentation): make room and try again
                 with self._lock:
-                    evicted = self._evict_one(release_after)
-                if not evicted:
+                    victim = self._evict_one()
+                if victim is None:
                     raise
+                release_after(victim)
                 self.alloc_retries += 1
                 if self.release_wait is not None:
                     self.release_wait()
         with self._lock:
-            if vid in self._vols:  # loaded meanwhile by another request
-                release_after(dv)
-                return self._vols[vid]
-            self._vols[vid] = dv
-            self._bytes[vid] = dv.device_bytes()
-            self.loads += 1
-            self.uploaded_bytes += int(volume.data.nbytes)
+            other = self._vols.get(vid)
+            if other is None:
+                self._vols[vid] = dv
+                self._bytes[vid] = dv.device_bytes()
+                self.loads += 1
+                self.uploaded_bytes += int(volume.data.nbytes)
+        if other is not None:  # loaded meanwhile by another request
+            release_after(dv)
+            return other
         return dv
 
 
@@ -707,6 +718,10 @@ class NativeRenderServer:
         self._release_stream = torch.cuda.Stream()
         self.cache = VolumeCache(budget_bytes, brick_log2, half_records,
                                  release_wait=self._release_stream.synchronize)
+        # the volume memory pool holds the budget (and room for a layout in
+        # progress) from the start: loads and evictions then reuse pool
+        # memory instead of mapping new memory while renders run
+        _native.check(_native.load().pvr_reserve_volume_memory(int(budget_bytes * 1.1)))
         self.luts = LutCache()
         self.luts.reserve(256, lut_reserve)
         self.per_frame = per_frame
