@@ -72,7 +72,8 @@ template <> __device__ __forceinline__ uint2 make_record<uint2>(float v, float3 
 
 constexpr int kLayoutThreads = 256;
 
-// One block per brick (grid-stride over bricks).  The block first stages
+// One block per brick (grid-stride over bricks; launched with one block per
+// brick).  The block first stages
 // the brick's texels plus a two-texel margin ((B+3)^3, clamped to the
 // volume) in shared memory, then writes the brick's (B+1)^3 records: the
 // stored value and the normal (given: read from `nrm`; computed on the
@@ -251,7 +252,9 @@ template <typename T, int LOG2B>
 cudaError_t build_typed(const BrickGeometry &g, const void *vol, const int dims[3], const float *nrm,
                         int normals_mode, const uint32_t *table, void *records, bool half, uint4 *bricks,
                         cudaStream_t st) {
-    const int blocks = std::max(1, std::min(g.nbricks, 152 * 8));
+    // one block per brick: short blocks, so that render kernels on streams
+    // of higher priority get SMs as soon as any layout block retires
+    const int blocks = std::max(1, g.nbricks);
     if (half)
         build_bricks_kernel<T, LOG2B, uint2><<<blocks, kLayoutThreads, 0, st>>>(
             g, (const T *)vol, dims[0], dims[1], dims[2], nrm, normals_mode, table, (uint2 *)records, bricks);

@@ -310,9 +310,12 @@ int pvr_volume_create(const void *data, int dtype, int d, int h, int w, float va
         v->bmax[a] = max_bounds[a];
     }
     const size_t nvox = (size_t)d * h * w;
-    // a stream of its own: the load runs beside renders on other streams
+    // a stream of its own at the lowest priority: the load runs beside
+    // renders on other streams, whose blocks the device schedules first
     cudaStream_t st = nullptr;
-    cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    int prio_low = 0, prio_high = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
+    cudaError_t e = cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, prio_low);
     if (e != cudaSuccess) {
         delete v;
         return pvr::cuda_fail(e, "cudaStreamCreateWithFlags");

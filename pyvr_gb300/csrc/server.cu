@@ -390,7 +390,10 @@ int pvr_server_create(const pvr_server_config *cfg, pvr_server **out) {
     srv->slots.resize(srv->cfg.slots);
     int rc = PVR_OK;
     for (auto &s : srv->slots) {
-        cudaError_t e = cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking);
+        // renders take precedence over volume layouts (lowest priority)
+        int prio_low = 0, prio_high = 0;
+        cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
+        cudaError_t e = cudaStreamCreateWithPriority(&s.stream, cudaStreamNonBlocking, prio_high);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreate(&s.k0);
         if (e == cudaSuccess) e = cudaEventCreate(&s.k1);
