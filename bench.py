@@ -352,12 +352,17 @@ def serving_section(args, torch):
     def measure(impl, warm_seed):
         """Warm-up, the latency at the nominal rate, the untimed rate sweep and
         the timed steps of one implementation."""
+        def make_catalog_resident():
+            # untimed: the volumes of the catalog are the ones being served,
+            # resident in a running service (loaded before the stream starts)
+            for slot in range(wl.n_catalog):
+                vid = wl.catalog[slot]
+                vol, vs = wl.volumes[vid]
+                impl.cache.insert(vid, vol, vs, impl._free_volume)
+            torch.cuda.synchronize()
+
         wl.restore(start)
-        for slot in range(wl.n_catalog):
-            vid = wl.catalog[slot]
-            vol, vs = wl.volumes[vid]
-            impl.cache.insert(vid, vol, vs, impl._free_volume)
-        torch.cuda.synchronize()
+        make_catalog_resident()
         # warm-up: W untimed one-second segments at the nominal rate (the same
         # streams for both implementations)
         for w in range(args.warmup):
@@ -366,7 +371,13 @@ def serving_section(args, torch):
         # every stream: each measurement below restarts from this point, so
         # that all of them see the same mix
         snap = wl.snapshot()
-        reset = lambda: wl.restore(snap)  # noqa: E731
+
+        def reset():
+            # the same workload state (catalog, sessions) for every run, with
+            # the catalog resident as it was at the snapshot
+            wl.restore(snap)
+            make_catalog_resident()
+
         reset()
         reqs, el = drive(impl, wl.requests(NOMINAL_RATE, 3.0, 200))
         nominal = latency_stats(reqs)

@@ -706,11 +706,13 @@ class NativeRenderServer:
     allocated at start, so that new transfer functions are built into
     existing memory.  half_records: resident volumes whose values and normals
     are all halves exactly (float16 volumes with device normals) keep their
-    records as halves: half the memory, the same images.  close() frees the
+    records as halves: half the memory, the same images.  ``loaders``
+    threads upload and lay out new volumes (one measured best: concurrent
+    uploads of large volumes slow each other down).  close() frees the
     resident volumes and tables."""
 
     def __init__(self, budget_bytes: int = 40 << 30, max_batch: int = 64, slots: int = 8,
-                 tuning: Optional[Tuning] = None, brick_log2: int = 3, loaders: int = 2,
+                 tuning: Optional[Tuning] = None, brick_log2: int = 3, loaders: int = 1,
                  instrument: int = 0, per_frame: bool = False, linger_us: int = 0,
                  batch_pixels: int = 512 * 512, lut_reserve: int = 1024, half_records: bool = False):
         import torch
