@@ -372,7 +372,8 @@ typedef struct {
     int max_steps;
     int width, height;
     uint8_t *out_rgba8;         /* host, width*height*4 bytes, bottom row first */
-    int out_pinned;             /* 1: out_rgba8 is page-locked; the image is copied to it by DMA */
+    int out_pinned;             /* 1: out_rgba8 is page-locked (cudaHostAlloc / cudaHostRegister): the
+                                   march writes the image into it through its device mapping */
     void *wait_event;           /* cudaEvent_t the batch must wait for (e.g. the LUT's build), or NULL */
     unsigned long long tag;     /* echoed in the completion */
 } pvr_request;
