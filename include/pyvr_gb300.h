@@ -181,6 +181,15 @@ int pvr_volume_device_bytes(const pvr_volume *v, long long *bytes);
  * under a byte budget) take their memory from the pool instead of mapping
  * new memory while renders run.  No reference counterpart. */
 int pvr_reserve_volume_memory(long long bytes);
+/* Page-locked host memory for volume data (cudaHostAlloc, portable to every
+ * device), freed with pvr_host_free.  pvr_volume_create uploads from it at
+ * the link's full speed; on Grace-Blackwell, uploads from pageable memory
+ * registered with cudaHostRegister ran several times slower, with 10-70 ms
+ * tails for 100-250 MB volumes.  *out is NULL on failure (PVR_ERR_NOMEM when
+ * the memory is not available).  No reference counterpart (moderngl uploads
+ * from the numpy array, manager.py:88-97). */
+int pvr_host_alloc(long long bytes, void **out);
+int pvr_host_free(void *p);
 /* Bytes per texel record of the volume's layout: 16 (float value + float
  * normal) or 8 (the same four floats as halves, used when every one of them
  * is a half exactly -- float16 volumes with normals computed in half

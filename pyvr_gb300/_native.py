@@ -111,6 +111,8 @@ SIGNATURES = {
     "pvr_volume_records_exact": (_I, [_VP, ctypes.POINTER(_I)]),
     "pvr_set_arithmetic": (_I, [_I]),
     "pvr_reserve_volume_memory": (_I, [_LL]),
+    "pvr_host_alloc": (_I, [_LL, ctypes.POINTER(_VP)]),
+    "pvr_host_free": (_I, [_VP]),
     "pvr_get_arithmetic": (_I, [ctypes.POINTER(_I)]),
     "pvr_volume_compact": (_I, [_VP, ctypes.POINTER(_I)]),
     "pvr_render_pinned": (_I, [_VP, ctypes.POINTER(_VP)]),

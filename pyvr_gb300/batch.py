@@ -24,6 +24,42 @@ def _lib():
     return _native.load()
 
 
+class _PageLocked:
+    """One pvr_host_alloc block; freed when the last array viewing it goes."""
+
+    def __init__(self, nbytes: int):
+        p = ctypes.c_void_p()
+        check(_lib().pvr_host_alloc(int(nbytes), ctypes.byref(p)))
+        self.ptr, self.nbytes = p.value, int(nbytes)
+
+    def __del__(self):
+        if getattr(self, "ptr", None):
+            try:
+                _lib().pvr_host_free(ctypes.c_void_p(self.ptr))
+            except Exception:
+                pass
+            self.ptr = None
+
+
+def page_locked_empty(shape, dtype) -> np.ndarray:
+    """A numpy array in page-locked host memory (``pvr_host_alloc``):
+    volumes uploaded from it (``DeviceVolume``, the render server's loads)
+    move at the link's full speed.  The memory is freed with the array."""
+    dtype = np.dtype(dtype)
+    n = int(np.prod(shape)) * dtype.itemsize
+    owner = _PageLocked(max(n, 1))
+    buf = (ctypes.c_uint8 * max(n, 1)).from_address(owner.ptr)
+    buf._owner = owner  # the array's base (buf) keeps the block alive
+    return np.frombuffer(buf, dtype=np.uint8, count=n).view(dtype).reshape(shape)
+
+
+def page_locked_copy(a: np.ndarray) -> np.ndarray:
+    """``a`` copied into page-locked host memory (C order)."""
+    out = page_locked_empty(a.shape, a.dtype)
+    out[...] = a
+    return out
+
+
 class DeviceVolume:
     """A volume resident on the GPU in the march layout.
 

@@ -381,6 +381,28 @@ int pvr_reserve_volume_memory(long long bytes) {
     return PVR_OK;
 }
 
+int pvr_host_alloc(long long bytes, void **out) {
+    if (!out) return fail(PVR_ERR_VALUE, "NULL argument");
+    *out = nullptr;
+    if (bytes <= 0) return fail(PVR_ERR_VALUE, "bytes must be > 0");
+    cudaError_t e = cudaHostAlloc(out, (size_t)bytes, cudaHostAllocPortable);
+    if (e != cudaSuccess) {
+        *out = nullptr;
+        if (e == cudaErrorMemoryAllocation) {
+            cudaGetLastError();
+            return fail(PVR_ERR_NOMEM, "no page-locked host memory for %lld bytes", bytes);
+        }
+        return pvr::cuda_fail(e, "cudaHostAlloc");
+    }
+    return PVR_OK;
+}
+
+int pvr_host_free(void *p) {
+    if (!p) return PVR_OK;
+    PVR_CUDA(cudaFreeHost(p));
+    return PVR_OK;
+}
+
 int pvr_set_compact_records(int mode) {
     if (mode < PVR_RECORDS_FLOAT || mode > PVR_RECORDS_HALF_NORMALS)
         return fail(PVR_ERR_VALUE, "record mode must be 0 (float), 1 (half where exact) or 2 (half normals)");

@@ -63,6 +63,20 @@ def test_half_normal_records(dtype):
         assert nan_equal(dv.read_normals(), want.astype(np.float16).astype(np.float32))
 
 
+def test_page_locked_volume_data():
+    # volumes uploaded from pvr_host_alloc memory lay out like any other
+    from pyvr_gb300.batch import page_locked_copy, page_locked_empty
+    data = W.to_storage(W.value_noise((20, 22, 24), seed=6), "u8")
+    pl = page_locked_copy(data)
+    assert pl.dtype == data.dtype and pl.shape == data.shape and np.array_equal(pl, data)
+    a = DeviceVolume(Volume(data=data), normals="device", brick_log2=3)
+    b = DeviceVolume(Volume(data=pl), normals="device", brick_log2=3)
+    assert nan_equal(a.read_normals(), b.read_normals())
+    e = page_locked_empty((3, 4, 5), np.float16)
+    assert e.shape == (3, 4, 5) and e.dtype == np.float16
+    del pl, e  # freed with the arrays
+
+
 def test_given_normals_roundtrip():
     data = W.value_noise((9, 10, 11), seed=4)
     vol = Volume(data=data, normals=compute_normal_volume(data))
