@@ -66,6 +66,10 @@ SERVING_512_WARP_INSTR_PER_SAMPLE = 7.82
 SERVING_512_DRAM_BYTES_PER_SAMPLE = 23.4
 PLAIN_WARP_INSTR_PER_SAMPLE = 6.68
 PLAIN_DRAM_BYTES_PER_SAMPLE = 0.80
+# ... and of the persistent batch kernel on the 64 uneven renders
+# (profiles/march_batch_kernel_batching64.md)
+BATCH_WARP_INSTR_PER_SAMPLE = 7.20
+BATCH_DRAM_BYTES_PER_SAMPLE = 1.20
 P99_MS = 20.0
 # the requests whose latency the p99 bound applies to: the 512^2 frames
 # (orbit re-renders, TF edits, and the renders of newly loaded volumes, the
@@ -80,7 +84,8 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="oracle seconds of the CPU baseline")
-    ap.add_argument("--probe-s", type=float, default=2.0, help="seconds per rate probe")
+    ap.add_argument("--probe-s", type=float, default=0.0,
+                    help="seconds per rate probe (0: as long as the timed run, --steps seconds)")
     ap.add_argument("--refine", type=int, default=4, help="bisection probes after the doubling sweep")
     ap.add_argument("--slots", type=int, default=8, help="server: launches in flight (streams)")
     ap.add_argument("--max-batch", type=int, default=64, help="server: requests per launch")
@@ -102,6 +107,7 @@ def parse_args():
     ap.add_argument("--only", choices=["all", "plain", "serving", "diff", "batching", "loaders", "requests"],
                     default="all")
     ap.add_argument("--serving-min-dim", type=int, default=128)
+    ap.add_argument("--loaders", type=int, default=1, help="server: loader threads for new volumes")
     ap.add_argument("--requests", type=int, default=24, help="requests section: renders of the stream")
     ap.add_argument("--loaders-volume", type=int, default=256, help="loaders section: volume extent")
     ap.add_argument("--diff-steps", type=int, default=200, help="Adam steps of the differentiation section")
@@ -397,7 +403,10 @@ def serving_section(args, torch):
         # untimed sweep: highest rate with p99 <= 20 ms (a failing probe is
         # repeated once)
         rates = [NOMINAL_RATE * (2 ** k) for k in range(8)]
-        rate, probes = sustained_rate(impl, wl, rates, args.probe_s, 300, refine=args.refine, reset=reset,
+        # probes as long as the timed run: a loader that falls behind shows
+        # its queue only after a few seconds
+        probe_s = args.probe_s or float(args.steps)
+        rate, probes = sustained_rate(impl, wl, rates, probe_s, 300, refine=args.refine, reset=reset,
                                       bound_tags=FRAME_TAGS)
         reqs, el, st, attempts = timed_run(impl, rate or NOMINAL_RATE, 500, reset)
         return dict(nominal=nominal, probes=probes, reqs=reqs, el=el, stats=st, attempts=attempts,
@@ -408,7 +417,8 @@ def serving_section(args, torch):
     # the clocks are sampled during the timed steps of both
     server = NativeRenderServer(budget_bytes=40 << 30, max_batch=args.max_batch, slots=args.slots, instrument=8,
                                 batch_pixels=args.batch_pixels,
-                                linger_us=args.linger_us, brick_log2=args.serving_brick_log2)
+                                linger_us=args.linger_us, brick_log2=args.serving_brick_log2,
+                                loaders=args.loaders)
     srv = measure(server, 100)
     server.close()
     del server
@@ -585,11 +595,12 @@ def batching_section(args, torch):
             "tuning": dataclasses.asdict(best), "tuning_search_s": tune_s, "candidates": len(results),
             "candidate_ms": sorted(round(ms, 3) for _, ms in results)[:5],
             "samples_inbox": int(per[:, 0].sum()), "samples_shaded": int(per[:, 1].sum()),
-            "roofline": march_roofline(int(per[:, 1].sum()), ms_best / 1000.0, None, PLAIN_WARP_INSTR_PER_SAMPLE,
-                                       SERVING_DRAM_BYTES_PER_SAMPLE, shaded_bytes, torch,
+            "roofline": march_roofline(int(per[:, 1].sum()), ms_best / 1000.0, None, BATCH_WARP_INSTR_PER_SAMPLE,
+                                       BATCH_DRAM_BYTES_PER_SAMPLE, shaded_bytes, torch,
                                        kernel="march_batch_kernel", launches=1,
-                                       note="one batch launch; per-sample constants of the single-render "
-                                            "kernel (the batch kernel marches the same way)"),
+                                       note="one batch (a persistent launch per kernel variant) over its "
+                                            "CUDA-event time",
+                                       profile="profiles/march_batch_kernel_batching64.md"),
             "config": {"renders": len(scenes), "volumes": "32..384 per axis log-uniform, u8/f16/f32 value noise",
                        "resolutions": "128^2..1024^2", "render_config": "balanced", "steps": args.steps}}
 
@@ -1004,8 +1015,8 @@ def serving_config(args):
             "step": "one second of the request stream at the sustained rate",
             "sustained": f"highest offered rate with p99 <= {P99_MS:.0f} ms over the 512^2 frames (orbit, TF "
                          f"edit, and new-volume load then render; captures reported beside) and completions >= 0.9x "
-                         f"offered, found by an untimed sweep (doubling from {NOMINAL_RATE:.0f} req/s, "
-                         f"then {args.refine} bisection probes)",
+                         f"offered, found by an untimed sweep of {args.probe_s or args.steps:g}-second probes "
+                         f"(doubling from {NOMINAL_RATE:.0f} req/s, then {args.refine} bisection probes)",
             "server": (f"continuous batching over {args.slots} launch slots (streams), "
                        f"up to {args.max_batch} requests and {args.batch_pixels} pixels per launch, "
                        f"linger {args.linger_us} us, {args.records} records, {args.arithmetic} arithmetic; "

@@ -310,12 +310,14 @@ int pvr_volume_create(const void *data, int dtype, int d, int h, int w, float va
         v->bmax[a] = max_bounds[a];
     }
     const size_t nvox = (size_t)d * h * w;
-    // a stream of its own at the lowest priority: the load runs beside
-    // renders on other streams, whose blocks the device schedules first
+    // a stream of its own at the highest priority: a load holds the renders
+    // queued meanwhile back by the layout's few milliseconds, while at the
+    // lowest priority it waited behind render launches for tens of
+    // milliseconds, and with it every request for the new volume
     cudaStream_t st = nullptr;
     int prio_low = 0, prio_high = 0;
     cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
-    cudaError_t e = cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, prio_low);
+    cudaError_t e = cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, prio_high);
     if (e != cudaSuccess) {
         delete v;
         return pvr::cuda_fail(e, "cudaStreamCreateWithFlags");
