@@ -108,6 +108,8 @@ def parse_args():
                     default="all")
     ap.add_argument("--serving-min-dim", type=int, default=128)
     ap.add_argument("--loaders", type=int, default=1, help="server: loader threads for new volumes")
+    ap.add_argument("--switch-interval-us", type=float, default=0.0,
+                    help="serving: Python thread switch interval during the replays (0: unchanged)")
     ap.add_argument("--requests", type=int, default=24, help="requests section: renders of the stream")
     ap.add_argument("--loaders-volume", type=int, default=256, help="loaders section: volume extent")
     ap.add_argument("--diff-steps", type=int, default=200, help="Adam steps of the differentiation section")
@@ -330,6 +332,8 @@ def serving_section(args, torch):
             "device_bytes_estimate": int(sum(est.estimate_bytes(v) - v.data.nbytes for v, _ in wl.volumes)),
             "budget_bytes": 40 << 30}
     clocks = ClockSampler(gpu_index(dist_env()[2]))
+    if args.switch_interval_us:
+        sys.setswitchinterval(args.switch_interval_us * 1e-6)
 
     def timed_run(impl, rate, seed, reset):
         """K one-second steps at `rate`; a run whose p99 exceeds the bound is
@@ -360,7 +364,8 @@ def serving_section(args, torch):
                              "alloc_retries": c.alloc_retries - ar0,
                              "load_requests": sum(r.tag == "load" for r in reqs),
                              "load_p50_ms": load_lat.get("p50_ms"), "load_p99_ms": load_lat.get("p99_ms"),
-                             "resident_bytes": c.used})
+                             "resident_bytes": c.used,
+                             "device_free_bytes": int(torch.cuda.mem_get_info()[0])})
             # the ranks repeat together, so that their barriers stay paired
             if all_ok(frames.get("p99_ms", 1e9) <= P99_MS, device="cuda"):
                 break

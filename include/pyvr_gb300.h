@@ -381,8 +381,10 @@ typedef struct {
     int max_steps;
     int width, height;
     uint8_t *out_rgba8;         /* host, width*height*4 bytes, bottom row first */
-    int out_pinned;             /* 1: out_rgba8 is page-locked (cudaHostAlloc / cudaHostRegister): the
-                                   march writes the image into it through its device mapping */
+    int out_pinned;             /* 1: out_rgba8 is page-locked; the image is copied to it by DMA (the
+                                   march writing it through the host mapping instead, with 32-byte
+                                   rows over the chip-to-chip link, slowed concurrent uploads and
+                                   renders several-fold on Grace-Blackwell) */
     void *wait_event;           /* cudaEvent_t the batch must wait for (e.g. the LUT's build), or NULL */
     unsigned long long tag;     /* echoed in the completion */
 } pvr_request;

@@ -73,7 +73,6 @@ struct Slot {
     unsigned long long *h_counters = nullptr;
     std::vector<Req> reqs;
     std::vector<size_t> offs;
-    std::vector<char> direct;  // request i written by the march into its page-locked destination
     std::vector<pvr_job> jobs;
     int status = PVR_OK;
     bool instrumented = false;  // this batch records kernel events and counters
@@ -194,22 +193,9 @@ int launch_slot(pvr_server *srv, Slot &s) {
         for (int k = 0; k < i && !seen; ++k) seen = s.reqs[k].r.wait_event == ev;
         if (ev && !seen) PVR_CUDA(cudaStreamWaitEvent(s.stream, (cudaEvent_t)ev, 0));
     }
-    // a page-locked destination is written by the march itself, through its
-    // device mapping (Grace-Blackwell reaches host memory over the
-    // chip-to-chip link): no copy-engine work per request, whose copies
-    // would otherwise queue with the volume uploads; other destinations get
-    // their image through the slot's device arena
-    s.direct.assign(n, 0);
     for (int i = 0; i < n; ++i) {
         fill_from_request(s.reqs[i].r, s.jobs[i]);
-        void *dst = nullptr;
-        if (s.reqs[i].r.out_pinned && cudaHostGetDevicePointer(&dst, s.reqs[i].r.out_rgba8, 0) == cudaSuccess) {
-            s.jobs[i].d_rgba8 = dst;
-            s.direct[i] = 1;
-        } else {
-            cudaGetLastError();  // not mapped: the copy below
-            s.jobs[i].d_rgba8 = (char *)s.d_arena + s.offs[i];
-        }
+        s.jobs[i].d_rgba8 = (char *)s.d_arena + s.offs[i];
         s.jobs[i].d_counters = s.instrumented ? s.d_counters + 2 * i : nullptr;
     }
     if (s.instrumented) {
@@ -227,7 +213,6 @@ int launch_slot(pvr_server *srv, Slot &s) {
     bool staged = false;
     for (int i = 0; i < n; ++i) {
         const pvr_request &r = s.reqs[i].r;
-        if (s.direct[i]) continue;
         if (r.out_pinned)
             PVR_CUDA(cudaMemcpyAsync(r.out_rgba8, (const char *)s.d_arena + s.offs[i], (size_t)r.width * r.height * 4,
                                      cudaMemcpyDeviceToHost, s.stream));
