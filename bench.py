@@ -35,6 +35,7 @@ all host cores) rendering whole frames of the same request mix.
 import argparse
 import ctypes
 import dataclasses
+import gc
 import json
 import os
 import statistics
@@ -1045,20 +1046,31 @@ def run_ours(args):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
-    plain = plain_section(args, torch) if args.only in ("all", "plain") else None
-    diff = diff_section(args, torch) if args.only in ("all", "diff") else None
-    batching = batching_section(args, torch) if args.only in ("all", "batching") else None
-    loaders = loaders_section(args, torch) if args.only in ("all", "loaders") else None
     if args.only == "requests":
         if rank == 0:
             print(json.dumps({"requests": requests_section(args, torch)}))
         return
-    if args.only in ("plain", "diff", "batching", "loaders"):
+    # the headline first, in a fresh process (no state of the other sections
+    # -- their device memory, host threads, collected garbage -- around it)
+    s = serving_section(args, torch) if args.only in ("all", "serving") else None
+
+    def section(name, fn):
+        if args.only not in ("all", name):
+            return None
+        gc.collect()
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+        return fn(args, torch)
+
+    plain = section("plain", plain_section)
+    diff = section("diff", diff_section)
+    batching = section("batching", batching_section)
+    loaders = section("loaders", loaders_section)
+    if s is None:
         if rank == 0:
             print(json.dumps({"plain": plain, "differentiation": diff, "batching_c3": batching,
                               "loaders": loaders}))
         return
-    s = serving_section(args, torch)
     value, serial_value = s["value"], s["serial_value"]
     if world > 1:
         # replicas: each rank serves its own stream; the job's rate is all the
