@@ -169,6 +169,21 @@ int pvr_frame_constants(const float view[16], const float proj[16], const float 
 int pvr_volume_create(const void *data, int dtype, int d, int h, int w, float value_scale,
                       const float min_bounds[3], const float max_bounds[3], const float *normals,
                       int normals_mode, int brick_log2, pvr_volume **out);
+/* As pvr_volume_create, but returns once the upload and the layout are
+ * queued (on a stream of the volume's own, at the highest priority) instead
+ * of when they are done: a serving loader hands the volume on at once, and
+ * every render, batch and release of the volume waits on the device for its
+ * layout (the server, pvr_batch_render and pvr_batch_render_static do this
+ * themselves).  `data` (and `normals`) must stay valid and unchanged until
+ * pvr_volume_ready reports 1.  Layouts of pvr_set_compact_records(1) keep
+ * their float records here (that compaction needs the finished layout).  No
+ * reference counterpart. */
+int pvr_volume_create_async(const void *data, int dtype, int d, int h, int w, float value_scale,
+                            const float min_bounds[3], const float max_bounds[3], const float *normals,
+                            int normals_mode, int brick_log2, pvr_volume **out);
+/* *ready = 1 once the volume's layout has completed (always for volumes
+ * from pvr_volume_create), else 0. */
+int pvr_volume_ready(const pvr_volume *v, int *ready);
 int pvr_volume_destroy(pvr_volume *v);   /* waits for the whole device first */
 /* Free the volume's memory in order on `stream` without waiting: the caller
  * makes `stream` wait for every batch that reads the volume.  The handle is

@@ -112,6 +112,8 @@ SIGNATURES = {
     "pvr_set_arithmetic": (_I, [_I]),
     "pvr_reserve_volume_memory": (_I, [_LL]),
     "pvr_host_alloc": (_I, [_LL, ctypes.POINTER(_VP)]),
+    "pvr_volume_create_async": (_I, [_VP, _I, _I, _I, _I, _F, _FP, _FP, _VP, _I, _I, ctypes.POINTER(_VP)]),
+    "pvr_volume_ready": (_I, [_VP, ctypes.POINTER(_I)]),
     "pvr_host_free": (_I, [_VP]),
     "pvr_get_arithmetic": (_I, [ctypes.POINTER(_I)]),
     "pvr_volume_compact": (_I, [_VP, ctypes.POINTER(_I)]),

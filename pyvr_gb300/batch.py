@@ -70,7 +70,7 @@ class DeviceVolume:
     """
 
     def __init__(self, volume, value_scale: float = 1.0, normals: str = "auto",
-                 brick_log2: int = 0, half_records: bool = False):
+                 brick_log2: int = 0, half_records: bool = False, wait: bool = True):
         data, code = volume_storage(np.asarray(volume.data))
         mode = normals
         if mode == "auto":
@@ -91,10 +91,13 @@ class DeviceVolume:
         bmax = np.asarray(volume.max_bounds, dtype=np.float32)
         h = ctypes.c_void_p()
         d0, d1, d2 = data.shape
-        check(_lib().pvr_volume_create(data.ctypes.data, code, d0, d1, d2, float(value_scale),
-                                       _native.fptr(bmin), _native.fptr(bmax), nrm_ptr, codes[mode],
-                                       int(brick_log2), ctypes.byref(h)))
-        self._keep = None
+        # wait=False: the upload and layout are only queued (the renders of
+        # the volume wait for them on the device); the host arrays stay
+        # referenced until ready() has seen the layout complete
+        create = _lib().pvr_volume_create if wait else _lib().pvr_volume_create_async
+        check(create(data.ctypes.data, code, d0, d1, d2, float(value_scale), _native.fptr(bmin),
+                     _native.fptr(bmax), nrm_ptr, codes[mode], int(brick_log2), ctypes.byref(h)))
+        self._keep = None if wait else (data, self._keep)
         self.handle = h
         self.shape = data.shape
         self.dtype = data.dtype
@@ -102,6 +105,14 @@ class DeviceVolume:
         self.brick_log2 = brick_log2 or 3
         if half_records:
             self.compact()
+
+    def ready(self) -> bool:
+        """True once the layout has completed (always after wait=True)."""
+        r = ctypes.c_int(0)
+        check(_lib().pvr_volume_ready(self.handle, ctypes.byref(r)))
+        if r.value:
+            self._keep = None
+        return bool(r.value)
 
     def compact(self) -> bool:
         """Records as halves if every one of their floats is a half exactly

@@ -312,6 +312,9 @@ int pvr_batch_render(pvr_batch *b, const pvr_job *jobs, int n, void *stream) {
             return fail(PVR_ERR_VALUE, "all volumes of a batch must share one brick size");
     }
     cudaStream_t st = stream ? (cudaStream_t)stream : b->stream;
+    // volumes whose layout may still run (pvr_volume_create_async)
+    for (int i = 0; i < n; ++i)
+        if (i == 0 || jobs[i].volume != jobs[i - 1].volume) pvr::volume_stream_wait(jobs[i].volume, st);
     const bool fast = pvr::arithmetic_fast();  // one arithmetic for the whole call
     // one launch (or more, of at most kMaxLaunchJobs) per kernel variant
     std::vector<int> groups[16];

@@ -168,6 +168,22 @@ extern "C" int pvr_batch_render_static(const pvr_job *jobs, int n, const pvr_tun
             return fail(rc, "job %d: %s", i, why.c_str());
         }
     }
+    // volumes whose layout may still run (pvr_volume_create_async): the
+    // stream waits for them; under stream capture, whose graph cannot wait on
+    // work queued outside it, every layout must have completed
+    cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+    PVR_CUDA(cudaStreamIsCapturing(st, &capture));
+    for (int i = 0; i < n; ++i) {
+        const pvr_volume *v = jobs[i].volume;
+        if (i > 0 && v == jobs[i - 1].volume) continue;
+        if (capture != cudaStreamCaptureStatusNone) {
+            if (v->ready && !v->ready_done.load())
+                return fail(PVR_ERR_STATE, "job %d: the volume's layout may still be running (wait for "
+                                           "pvr_volume_ready before capturing)", i);
+        } else {
+            pvr::volume_stream_wait(v, st);
+        }
+    }
     for (int v = 0, c = 0; v < kVariants; ++v) {
         for (int i0 = start[v]; i0 < start[v + 1]; i0 += pvr::kMaxLaunchJobs) {
             const int m = std::min(pvr::kMaxLaunchJobs, start[v + 1] - i0);

@@ -1,6 +1,8 @@
 // Host/device declarations shared between the C-ABI layer and the kernels.
 #pragma once
 
+#include <atomic>
+
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -144,7 +146,11 @@ struct pvr_volume {
     bool compact_exact = true;  // ... and every float of them survived exactly
     uint32_t *d_table = nullptr;  // brick -> record slot
     uint4 *d_bricks = nullptr;    // brick -> {slot, min, max}
-    bool layout_ready = false;
+    bool layout_ready = false;    // the layout is built or queued
+    // recorded after the layout's work (volumes created by pvr_volume_create*):
+    // device work on the volume waits for it; ready_done once it has completed
+    cudaEvent_t ready = nullptr;
+    mutable std::atomic<bool> ready_done{false};
 };
 
 struct pvr_lut {
@@ -160,6 +166,8 @@ namespace pvr {
 int fail(int code, const char *fmt, ...);
 int cuda_fail(cudaError_t e, const char *what);
 int ensure_volume_layout(pvr_volume *v, cudaStream_t st);
+// Make `st` wait for the volume's layout if it may still be running.
+void volume_stream_wait(const pvr_volume *v, cudaStream_t st);
 int try_compact_records(pvr_volume *v, cudaStream_t st, bool round_normals);
 cudaError_t vol_alloc(void **p, size_t bytes, cudaStream_t st);
 void vol_free(void *p, cudaStream_t st);

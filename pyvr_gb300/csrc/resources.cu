@@ -127,9 +127,10 @@ static std::atomic<int> g_arithmetic{PVR_ARITH_FAST};
 
 bool arithmetic_fast() { return g_arithmetic.load(std::memory_order_relaxed) == PVR_ARITH_FAST; }
 
-// Records, brick table and value ranges of a volume (once per volume).
-int ensure_volume_layout(pvr_volume *v, cudaStream_t st) {
-    if (v->layout_ready) return PVR_OK;
+// The allocations of a volume's layout and the upload of its brick table
+// (from pageable memory: on a stream with no work queued yet, the copy is
+// staged and returns at once).
+static int layout_prepare(pvr_volume *v, cudaStream_t st, bool &half) {
     vol_free(v->d_records, st);
     vol_free(v->d_table, st);
     vol_free(v->d_bricks, st);
@@ -140,17 +141,22 @@ int ensure_volume_layout(pvr_volume *v, cudaStream_t st) {
     v->geo = make_brick_geometry(v->dims, v->log2b);
     std::vector<uint32_t> table = morton_slots(v->geo);
     const size_t nrec = (size_t)v->geo.nbricks * brick_records(v->log2b);
-    const int mode = g_compact_records.load();
     // half records written directly: values of uint8 / float16 volumes are
     // halves exactly; normals are rounded to half
-    const bool half = mode == PVR_RECORDS_HALF_NORMALS && v->dtype != PVR_F32;
+    half = g_compact_records.load() == PVR_RECORDS_HALF_NORMALS && v->dtype != PVR_F32;
     const size_t rec_size = half ? sizeof(uint2) : sizeof(float4);
     PVR_CUDA(vol_alloc((void **)&v->d_records, nrec * rec_size, st));
     v->records_bytes = nrec * rec_size;
     PVR_CUDA(vol_alloc((void **)&v->d_table, table.size() * sizeof(uint32_t), st));
     PVR_CUDA(vol_alloc((void **)&v->d_bricks, table.size() * sizeof(uint4), st));
+    // pageable source: staged before the call returns, so `table` may go
     PVR_CUDA(cudaMemcpyAsync(v->d_table, table.data(), table.size() * sizeof(uint32_t),
                              cudaMemcpyHostToDevice, st));
+    return PVR_OK;
+}
+
+// The layout kernel over the uploaded voxels (and given normals).
+static int layout_launch(pvr_volume *v, cudaStream_t st, bool half) {
     PVR_CUDA(launch_build_records(v->geo, v->dtype, v->d_vol, v->dims, v->d_nrm, v->normals_mode,
                                   v->d_table, v->d_records, half, v->d_bricks, st));
     vol_free(v->d_nrm, st);  // given normals now live in the records
@@ -160,10 +166,29 @@ int ensure_volume_layout(pvr_volume *v, cudaStream_t st) {
     // precision (numpy's arithmetic for float16 input)
     v->compact_exact = !half || v->normals_mode == PVR_NORMALS_NONE ||
                        (v->dtype == PVR_F16 && v->normals_mode == PVR_NORMALS_DEVICE);
-    PVR_CUDA(cudaStreamSynchronize(st));  // `table` leaves scope; ready for any stream
-    v->layout_ready = true;
-    if (mode == PVR_RECORDS_HALF_EXACT) try_compact_records(v, st, false);
     return PVR_OK;
+}
+
+// Records, brick table and value ranges of a volume (once per volume).
+int ensure_volume_layout(pvr_volume *v, cudaStream_t st) {
+    if (v->layout_ready) return PVR_OK;
+    bool half = false;
+    if (int rc = layout_prepare(v, st, half)) return rc;
+    if (int rc = layout_launch(v, st, half)) return rc;
+    PVR_CUDA(cudaStreamSynchronize(st));  // ready for any stream
+    v->layout_ready = true;
+    if (g_compact_records.load() == PVR_RECORDS_HALF_EXACT) try_compact_records(v, st, false);
+    return PVR_OK;
+}
+
+void volume_stream_wait(const pvr_volume *v, cudaStream_t st) {
+    if (!v || !v->ready || v->ready_done.load(std::memory_order_acquire)) return;
+    if (cudaEventQuery(v->ready) == cudaSuccess) {
+        v->ready_done.store(true, std::memory_order_release);
+        return;
+    }
+    cudaGetLastError();  // cudaErrorNotReady
+    cudaStreamWaitEvent(st, v->ready, 0);
 }
 
 // Half records when every value and normal is a half exactly: float16
@@ -272,9 +297,9 @@ int pvr_abi_version(void) { return PVR_ABI_VERSION; }
 
 const char *pvr_last_error(void) { return g_last_error.c_str(); }
 
-int pvr_volume_create(const void *data, int dtype, int d, int h, int w, float value_scale,
-                      const float min_bounds[3], const float max_bounds[3], const float *normals,
-                      int normals_mode, int brick_log2, pvr_volume **out) {
+static int create_volume(const void *data, int dtype, int d, int h, int w, float value_scale,
+                         const float min_bounds[3], const float max_bounds[3], const float *normals,
+                         int normals_mode, int brick_log2, bool async, pvr_volume **out) {
     if (!out) return fail(PVR_ERR_VALUE, "out is NULL");
     *out = nullptr;
     if (!data) return fail(PVR_ERR_VALUE, "volume data is NULL");
@@ -323,12 +348,18 @@ int pvr_volume_create(const void *data, int dtype, int d, int h, int w, float va
         return pvr::cuda_fail(e, "cudaStreamCreateWithFlags");
     }
     auto bail = [&](int rc) {
+        cudaStreamSynchronize(st);
         pvr::free_volume_buffers(v, st);
         cudaStreamSynchronize(st);
         cudaStreamDestroy(st);
+        if (v->ready) cudaEventDestroy(v->ready);
         delete v;
         return rc;
     };
+    // the brick table first, while the stream is empty (its pageable copy
+    // then returns at once), then the voxels in their storage type
+    bool half = false;
+    if (int rc = pvr::layout_prepare(v, st, half)) return bail(rc);
     e = pvr::vol_alloc(&v->d_vol, nvox * dtype_size(dtype), st);
     if (e != cudaSuccess) return bail(pvr::cuda_fail(e, "allocate volume"));
     v->vol_bytes = nvox * dtype_size(dtype);
@@ -340,16 +371,56 @@ int pvr_volume_create(const void *data, int dtype, int d, int h, int w, float va
         e = cudaMemcpyAsync(v->d_nrm, normals, nvox * 3 * sizeof(float), cudaMemcpyHostToDevice, st);
         if (e != cudaSuccess) return bail(pvr::cuda_fail(e, "upload normals"));
     }
-    if (int rc = pvr::ensure_volume_layout(v, st)) return bail(rc);
+    if (int rc = pvr::layout_launch(v, st, half)) return bail(rc);
     // the records hold every stored value: the uploaded voxels are not needed
     // again (a volume resource is never laid out twice)
     pvr::vol_free(v->d_vol, st);
     v->d_vol = nullptr;
     v->vol_bytes = 0;
-    cudaStreamSynchronize(st);
-    cudaStreamDestroy(st);
+    e = cudaEventCreateWithFlags(&v->ready, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventRecord(v->ready, st);
+    if (e != cudaSuccess) return bail(pvr::cuda_fail(e, "record the layout's event"));
+    v->layout_ready = true;  // queued: device work on the volume waits for `ready`
+    if (!async) {
+        e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return bail(pvr::cuda_fail(e, "volume layout"));
+        v->ready_done.store(true);
+        if (pvr::g_compact_records.load() == PVR_RECORDS_HALF_EXACT) pvr::try_compact_records(v, st, false);
+    }
+    cudaStreamDestroy(st);  // its queued work still runs
     *out = v;
     return PVR_OK;
+}
+
+int pvr_volume_create(const void *data, int dtype, int d, int h, int w, float value_scale,
+                      const float min_bounds[3], const float max_bounds[3], const float *normals,
+                      int normals_mode, int brick_log2, pvr_volume **out) {
+    return create_volume(data, dtype, d, h, w, value_scale, min_bounds, max_bounds, normals, normals_mode,
+                         brick_log2, false, out);
+}
+
+int pvr_volume_create_async(const void *data, int dtype, int d, int h, int w, float value_scale,
+                            const float min_bounds[3], const float max_bounds[3], const float *normals,
+                            int normals_mode, int brick_log2, pvr_volume **out) {
+    return create_volume(data, dtype, d, h, w, value_scale, min_bounds, max_bounds, normals, normals_mode,
+                         brick_log2, true, out);
+}
+
+int pvr_volume_ready(const pvr_volume *v, int *ready) {
+    if (!v || !ready) return fail(PVR_ERR_VALUE, "NULL argument");
+    *ready = 1;
+    if (!v->ready || v->ready_done.load()) return PVR_OK;
+    const cudaError_t e = cudaEventQuery(v->ready);
+    if (e == cudaSuccess) {
+        v->ready_done.store(true);
+        return PVR_OK;
+    }
+    if (e == cudaErrorNotReady) {
+        cudaGetLastError();
+        *ready = 0;
+        return PVR_OK;
+    }
+    return pvr::cuda_fail(e, "volume layout");
 }
 
 int pvr_volume_destroy(pvr_volume *v) {
@@ -357,13 +428,17 @@ int pvr_volume_destroy(pvr_volume *v) {
     cudaDeviceSynchronize();  // no batch may still read it
     pvr::free_volume_buffers(v, 0);
     cudaDeviceSynchronize();
+    if (v->ready) cudaEventDestroy(v->ready);
     delete v;
     return PVR_OK;
 }
 
 int pvr_volume_release(pvr_volume *v, void *stream) {
     if (!v) return PVR_OK;
+    // behind the layout too, when it may still be running
+    pvr::volume_stream_wait(v, (cudaStream_t)stream);
     pvr::free_volume_buffers(v, (cudaStream_t)stream);
+    if (v->ready) cudaEventDestroy(v->ready);  // released once it has completed
     delete v;
     return PVR_OK;
 }
@@ -481,6 +556,7 @@ int pvr_volume_device_bytes(const pvr_volume *v, long long *bytes) {
 int pvr_volume_read_normals(const pvr_volume *v, float *normals_out) {
     if (!v || !normals_out) return fail(PVR_ERR_VALUE, "NULL argument");
     if (!v->layout_ready) return fail(PVR_ERR_STATE, "volume layout not built");
+    if (v->ready) PVR_CUDA(cudaEventSynchronize(v->ready));
     const size_t n = (size_t)v->dims[0] * v->dims[1] * v->dims[2] * 3;
     float *d = nullptr;
     PVR_CUDA(cudaMalloc(&d, n * sizeof(float)));

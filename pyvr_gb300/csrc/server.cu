@@ -192,6 +192,9 @@ int launch_slot(pvr_server *srv, Slot &s) {
         bool seen = false;  // one wait per distinct event
         for (int k = 0; k < i && !seen; ++k) seen = s.reqs[k].r.wait_event == ev;
         if (ev && !seen) PVR_CUDA(cudaStreamWaitEvent(s.stream, (cudaEvent_t)ev, 0));
+        // a volume whose layout may still run (pvr_volume_create_async)
+        if (i == 0 || s.reqs[i].r.volume != s.reqs[i - 1].r.volume)
+            pvr::volume_stream_wait(s.reqs[i].r.volume, s.stream);
     }
     for (int i = 0; i < n; ++i) {
         fill_from_request(s.reqs[i].r, s.jobs[i]);

@@ -86,10 +86,14 @@ class VolumeCache:
     ``alloc_retries``) until it succeeds or nothing is left to evict."""
 
     def __init__(self, budget_bytes: int, brick_log2: int = 3, half_records: bool = False,
-                 release_wait=None):
+                 release_wait=None, queue_layouts: bool = False):
         self.budget = int(budget_bytes)
         self.brick_log2 = brick_log2
         self.half_records = half_records
+        # queue_layouts: insert() returns once a new volume's upload and
+        # layout are queued (DeviceVolume(wait=False)); its renders wait for
+        # them on the device
+        self.queue_layouts = queue_layouts
         # release_wait(): wait until the memory of volumes released so far is
         # free again (before retrying a failed layout)
         self.release_wait = release_wait
@@ -192,7 +196,8 @@ class VolumeCache:
         while True:
             try:
                 dv = DeviceVolume(volume, value_scale=value_scale, normals=normals,
-                                  brick_log2=self.brick_log2, half_records=self.half_records)
+                                  brick_log2=self.brick_log2, half_records=self.half_records,
+                                  wait=not self.queue_layouts)
                 break
             except MemoryError:
                 # the device is fuller than the budget assumed (other memory
@@ -719,7 +724,7 @@ class NativeRenderServer:
         self.torch = torch
         self._release_stream = torch.cuda.Stream()
         self.cache = VolumeCache(budget_bytes, brick_log2, half_records,
-                                 release_wait=self._release_stream.synchronize)
+                                 release_wait=self._release_stream.synchronize, queue_layouts=True)
         # the volume memory pool holds the budget (and room for a layout in
         # progress) from the start: loads and evictions then reuse pool
         # memory instead of mapping new memory while renders run
@@ -800,7 +805,11 @@ class NativeRenderServer:
     # -- internals -----------------------------------------------------------------
     def _free_volume(self, dv: DeviceVolume) -> None:
         """An evicted volume: no request uses it any more (every batch that read
-        it has completed), so it is freed in the order of a private stream."""
+        it has completed), so it is freed in the order of a private stream
+        (behind its layout, if that is still queued).  Its host arrays are
+        let go only once the upload has read them."""
+        while not dv.ready():
+            time.sleep(0.0002)
         _native.check(self._lib.pvr_volume_release(dv.handle, self._release_stream.cuda_stream))
         dv.handle = None
 

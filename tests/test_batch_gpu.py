@@ -77,6 +77,43 @@ def test_page_locked_volume_data():
     del pl, e  # freed with the arrays
 
 
+@pytest.mark.parametrize("dtype", ["u8", "f32"])
+def test_queued_layout_renders_like_a_finished_one(dtype):
+    # pvr_volume_create_async: the batch launch waits on the device for the
+    # layout; images, normals and record form equal the synchronous volume's
+    data = W.to_storage(W.value_noise((48, 40, 44), seed=8), dtype)
+    vol = Volume(data=data)
+    a = DeviceVolume(vol, normals="device", brick_log2=3)
+    b = DeviceVolume(vol, normals="device", brick_log2=3, wait=False)
+    rng = np.random.default_rng(3)
+    lut = DeviceLUT(W.standin_colormap(3), W.random_opacity(rng, 8, 0.3))
+    cam = Camera.from_spherical(np.zeros(3, np.float32), 0.7, 0.4, 0.0, 3.0)
+    outs = []
+    br = BatchRenderer(capacity=4, slots=2)
+    for dv in (b, a):  # the queued volume first, straight after its creation
+        o8, of, _ = _job_outputs(64, 48)
+        br.render([RenderJob(dv, lut, cam, Light.directional([1, -1, 0], 0.2, 0.8), RenderConfig.balanced(),
+                             64, 48, o8, of)])
+        outs.append((o8, of))
+    torch.cuda.synchronize()
+    assert torch.equal(outs[0][0], outs[1][0]) and torch.equal(outs[0][1], outs[1][1])
+    assert b.ready() and b.record_bytes() == a.record_bytes()
+    assert nan_equal(a.read_normals(), b.read_normals())
+    br.close()
+
+
+def test_queued_layout_released_before_it_completes():
+    # a volume released right after its creation is freed behind its layout
+    from pyvr_gb300 import _native
+    data = W.to_storage(W.value_noise((96, 96, 96), seed=9), "f16")
+    dv = DeviceVolume(Volume(data=data), normals="device", brick_log2=4, wait=False)
+    s = torch.cuda.Stream()
+    _native.check(_native.load().pvr_volume_release(dv.handle, s.cuda_stream))
+    dv.handle = None
+    s.synchronize()
+    torch.cuda.synchronize()
+
+
 def test_given_normals_roundtrip():
     data = W.value_noise((9, 10, 11), seed=4)
     vol = Volume(data=data, normals=compute_normal_volume(data))

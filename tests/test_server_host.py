@@ -16,7 +16,8 @@ from pyvr_gb300 import workloads as W
 class FakeDeviceVolume:
     made = []
 
-    def __init__(self, volume, value_scale=1.0, normals="auto", brick_log2=0, half_records=False):
+    def __init__(self, volume, value_scale=1.0, normals="auto", brick_log2=0, half_records=False, wait=True):
+        self.waited = wait
         self.shape = volume.data.shape
         d, h, w = volume.data.shape
         lb = brick_log2 or 3  # the cache's own estimate of records + voxels
@@ -27,6 +28,9 @@ class FakeDeviceVolume:
 
     def device_bytes(self):
         return self.bytes
+
+    def ready(self):
+        return True
 
     def close(self):
         self.closed = True
@@ -88,6 +92,14 @@ def test_volume_cache_budget_lru_and_pins(fake_device):
     vols = [cache.get(i) for i in (1, 3, 4)]
     cache.clear()
     assert all(v.closed for v in vols) and cache.used == 0
+
+
+def test_volume_cache_queues_layouts_when_asked(fake_device):
+    # the native server's cache hands new volumes on with their layout queued
+    # (DeviceVolume(wait=False)); the default cache waits for it
+    S.VolumeCache(budget_bytes=1 << 30, brick_log2=3).insert(1, _vol(8), 1.0, lambda dv: None)
+    S.VolumeCache(budget_bytes=1 << 30, brick_log2=3, queue_layouts=True).insert(2, _vol(8), 1.0, lambda dv: None)
+    assert [v.waited for v in FakeDeviceVolume.made] == [True, False]
 
 
 def test_volume_cache_evicts_and_retries_when_allocation_fails(fake_device, monkeypatch):
