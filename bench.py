@@ -302,13 +302,15 @@ def reference_serving_steps(wl, steps, seconds_per_step, seed, server=None):
 
 def pin_host_volumes(workload):
     """The host copies of the volumes (the data a client hands in) in
-    page-locked memory from pvr_host_alloc.  (Registering the numpy arrays
-    with cudaHostRegister instead made uploads of 100-250 MB volumes take
-    10-70 ms at times on Grace-Blackwell, against about 1-2 ms from this
-    memory.)"""
-    from pyvr_gb300.batch import page_locked_copy
-    for vol, _ in workload.volumes:
-        vol.data = page_locked_copy(vol.data)
+    page-locked memory from pvr_host_alloc, all in one allocation.
+    (Registering the numpy arrays with cudaHostRegister instead made uploads
+    of 100-250 MB volumes take 10-70 ms at times on Grace-Blackwell, against
+    about 1-2 ms from this memory.)"""
+    from pyvr_gb300.batch import PageLockedArena
+    vols = [vol for vol, _ in workload.volumes]
+    arena = PageLockedArena(PageLockedArena.size_for([v.data for v in vols]))
+    for vol in vols:
+        vol.data = arena.copy(vol.data)
 
 
 def serving_section(args, torch):
@@ -344,11 +346,11 @@ def serving_section(args, torch):
         for _ in range(8):
             torch.cuda.synchronize()
             barrier()
+            reset()
             impl.reset_stats()
             c = impl.cache
             m0, up0, ld0, ev0, ob0, ar0 = (impl.luts.misses, c.uploaded_bytes, c.loads, c.evictions,
                                            c.over_budget, c.alloc_retries)
-            reset()
             clocks.start()
             reqs, el = drive(impl, wl.requests(rate, float(args.steps), seed))
             torch.cuda.synchronize()
@@ -377,12 +379,23 @@ def serving_section(args, torch):
         """Warm-up, the latency at the nominal rate, the untimed rate sweep and
         the timed steps of one implementation."""
         def make_catalog_resident():
-            # untimed: the volumes of the catalog are the ones being served,
-            # resident in a running service (loaded before the stream starts)
+            # untimed: the steady state of a running service with a full
+            # cache -- the catalog's volumes (the ones being served), then the
+            # volumes that left the catalog most recently, up to the budget;
+            # anything else (e.g. admitted over the budget while requests in
+            # flight pinned every volume) is let go first
+            cache = impl.cache
+            for dv in cache.evict_except(set(wl.catalog)):
+                impl._free_volume(dv)
             for slot in range(wl.n_catalog):
                 vid = wl.catalog[slot]
                 vol, vs = wl.volumes[vid]
-                impl.cache.insert(vid, vol, vs, impl._free_volume)
+                cache.insert(vid, vol, vs, impl._free_volume)
+            for vid in reversed(wl.outside):
+                vol, vs = wl.volumes[vid]
+                if cache.used + cache.estimate_bytes(vol) > cache.budget:
+                    break
+                cache.insert(vid, vol, vs, impl._free_volume)
             torch.cuda.synchronize()
 
         wl.restore(start)

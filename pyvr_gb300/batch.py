@@ -53,6 +53,39 @@ def page_locked_empty(shape, dtype) -> np.ndarray:
     return np.frombuffer(buf, dtype=np.uint8, count=n).view(dtype).reshape(shape)
 
 
+class PageLockedArena:
+    """One pvr_host_alloc block handing out numpy arrays (``array``), each at
+    a 4 KiB boundary: many volumes in one page-locked allocation instead of
+    one each.  The block is freed when the arena and every array from it
+    are gone."""
+
+    ALIGN = 4096
+
+    def __init__(self, nbytes: int):
+        self._owner = _PageLocked(max(int(nbytes), 1))
+        self._off = 0
+
+    @classmethod
+    def size_for(cls, arrays) -> int:
+        """Bytes an arena needs to hold copies of ``arrays``."""
+        return sum((int(a.nbytes) + cls.ALIGN - 1) // cls.ALIGN * cls.ALIGN for a in arrays)
+
+    def array(self, shape, dtype) -> np.ndarray:
+        dtype = np.dtype(dtype)
+        n = int(np.prod(shape)) * dtype.itemsize
+        if self._off + n > self._owner.nbytes:
+            raise MemoryError(f"page-locked arena of {self._owner.nbytes} bytes is full")
+        buf = (ctypes.c_uint8 * max(n, 1)).from_address(self._owner.ptr + self._off)
+        buf._owner = self._owner
+        self._off += (n + self.ALIGN - 1) // self.ALIGN * self.ALIGN
+        return np.frombuffer(buf, dtype=np.uint8, count=n).view(dtype).reshape(shape)
+
+    def copy(self, a: np.ndarray) -> np.ndarray:
+        out = self.array(a.shape, a.dtype)
+        out[...] = a
+        return out
+
+
 def page_locked_copy(a: np.ndarray) -> np.ndarray:
     """``a`` copied into page-locked host memory (C order)."""
     out = page_locked_empty(a.shape, a.dtype)

@@ -157,6 +157,17 @@ class VolumeCache:
         for dv in vols:
             dv.close()
 
+    def evict_except(self, keep) -> list:
+        """Take every volume whose id is not in ``keep`` and that no request
+        in flight uses out of the cache (without counting them as
+        evictions); the caller releases their memory."""
+        with self._lock:
+            out = []
+            for vid in [k for k in self._vols if k not in keep and self._users.get(k, 0) == 0]:
+                out.append(self._vols.pop(vid))
+                self._bytes.pop(vid)
+            return out
+
     def _evict_one(self):
         """Take the least recently used unpinned volume out of the cache (the
         caller releases its memory, outside the lock); None if none."""

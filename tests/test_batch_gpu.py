@@ -75,6 +75,16 @@ def test_page_locked_volume_data():
     e = page_locked_empty((3, 4, 5), np.float16)
     assert e.shape == (3, 4, 5) and e.dtype == np.float16
     del pl, e  # freed with the arrays
+    from pyvr_gb300.batch import PageLockedArena
+    arrays = [data, data.astype(np.float16)]
+    arena = PageLockedArena(PageLockedArena.size_for(arrays))
+    got = [arena.copy(a) for a in arrays]
+    assert all(np.array_equal(g, a) and g.dtype == a.dtype for g, a in zip(got, arrays))
+    assert got[1].ctypes.data % PageLockedArena.ALIGN == 0
+    with pytest.raises(MemoryError):
+        arena.array((1,), np.uint8)
+    c = DeviceVolume(Volume(data=got[0]), normals="device", brick_log2=3)
+    assert nan_equal(a.read_normals(), c.read_normals())
 
 
 @pytest.mark.parametrize("dtype", ["u8", "f32"])

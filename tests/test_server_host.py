@@ -94,6 +94,16 @@ def test_volume_cache_budget_lru_and_pins(fake_device):
     assert all(v.closed for v in vols) and cache.used == 0
 
 
+def test_volume_cache_evict_except_keeps_pinned_and_kept(fake_device):
+    cache = S.VolumeCache(budget_bytes=1 << 30, brick_log2=3)
+    for vid in range(4):
+        cache.insert(vid, _vol(8), 1.0, lambda dv: None)
+    cache.acquire(2)  # in flight: stays
+    out = cache.evict_except({0})
+    assert len(out) == 2 and sorted(cache._vols) == [0, 2]
+    assert cache.evictions == 0 and cache.used == sum(cache._bytes.values())
+
+
 def test_volume_cache_queues_layouts_when_asked(fake_device):
     # the native server's cache hands new volumes on with their layout queued
     # (DeviceVolume(wait=False)); the default cache waits for it
