@@ -393,7 +393,8 @@ int pvr_server_create(const pvr_server_config *cfg, pvr_server **out) {
     srv->slots.resize(srv->cfg.slots);
     int rc = PVR_OK;
     for (auto &s : srv->slots) {
-        // renders take precedence over volume layouts (lowest priority)
+        // at the highest priority, like volume layouts: renders of resident
+        // volumes go ahead of other work queued on the device
         int prio_low = 0, prio_high = 0;
         cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
         cudaError_t e = cudaStreamCreateWithPriority(&s.stream, cudaStreamNonBlocking, prio_high);
