@@ -1094,13 +1094,9 @@ def run_ours(args):
         serial_value = job_rate(n_ser, el_ser, device="cuda")
     cpu = None
     if rank == 0 and not args.skip_cpu:
-        steps, threads = reference_serving_steps(s["workload"], 1, args.cpu_seconds, 700)
-        nreq, ct, cn, nl = steps[0]
-        cpu = {"value": nreq / ct, "unit": "renders/s", "cores": threads, "kind": "port",
-               "sample": f"the reference's host path (float32 conversion and numpy normals for loads, "
-                         f"Camera matrices, host LUTs) and the oracle on whole frames: the first {nreq} "
-                         f"requests of a stream of the mix ({nl} loads) in {ct:.1f} s on {threads} threads",
-               "samples_per_s": cn / ct}
+        # the same sample as the reference arm (--impl reference)
+        c = reference_sample(args)
+        cpu = {k: c[k] for k in ("value", "unit", "cores", "kind", "sample", "samples_per_s")}
     if rank == 0:
         srv = s["server"]
         att, satt = s["attempts"]["server"][-1], s["attempts"]["serial"][-1]
@@ -1146,19 +1142,12 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
-def run_reference(args):
-    """The reference's own host path (no GPU, nothing of the pyvr_gb300 CUDA
-    library): float32 conversion and numpy normals for new volumes, the
-    Camera methods' matrices, host LUTs, and the CPU restatement of the
-    shader (the oracle) on all host cores, serving the same request mix one
-    request after another.  Each step is a bounded sample of the stream (at
-    least --cpu-seconds / --steps seconds of host work, one second at least);
-    the value is requests over the timed host seconds.  Volume data is
-    generated (numpy) and the catalog volumes a request finds resident get
-    their normals outside the timed work."""
-    rank, world, _ = dist_env()
-    if rank != 0:
-        return
+def reference_sample(args) -> dict:
+    """The reference's host path serving the request mix (ReferenceServer):
+    a fresh workload (numpy value noise), ``--warmup`` untimed steps of one
+    stream, then ``--steps`` timed steps of another, each at least
+    ``--cpu-seconds / --steps`` seconds of host work.  Both the reference arm
+    and the CPU baseline beside the headline report this same sample."""
     from pyvr_gb300 import workloads as W
     wl = W.ServingWorkload(n_volumes=args.serving_volumes, n_extra=args.serving_extra,
                            min_dim=args.serving_min_dim, max_dim=args.serving_max_dim, seed=0,
@@ -1172,17 +1161,38 @@ def run_reference(args):
     samples = sum(x for _, _, x, _ in steps)
     loads = sum(l for _, _, _, l in steps)
     value = reqs / secs if secs else 0.0
+    return {"value": value, "unit": "renders/s", "cores": threads, "kind": "port",
+            "sample": f"the reference's host path (float32 conversion and numpy normals for loads, Camera "
+                      f"matrices, host LUTs) and the oracle on whole frames: {len(steps)} steps of the mix in "
+                      f"stream order (catalog volumes {args.serving_min_dim}^3-{args.serving_max_dim}^3, 1024^2 "
+                      f"captures, new-volume loads), each "
+                      f">= {per_step:.1f} s of host work after {args.warmup} untimed steps; {reqs} requests "
+                      f"({loads} loads) in {secs:.1f} s on {threads} threads",
+            "samples_per_s": samples / secs if secs else 0.0,
+            "steps": len(steps), "seconds": secs}
+
+
+def run_reference(args):
+    """The reference's own host path (no GPU, nothing of the pyvr_gb300 CUDA
+    library): float32 conversion and numpy normals for new volumes, the
+    Camera methods' matrices, host LUTs, and the CPU restatement of the
+    shader (the oracle) on all host cores, serving the same request mix one
+    request after another.  Each step is a bounded sample of the stream (at
+    least --cpu-seconds / --steps seconds of host work, one second at least);
+    the value is requests over the timed host seconds.  Volume data is
+    generated (numpy) and the catalog volumes a request finds resident get
+    their normals outside the timed work."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    cpu = reference_sample(args)
+    value = cpu["value"]
     line = {"impl": "reference", "metric": "renders/s (batched server, mixed request stream, p99 of 512^2 frames <= 20 ms)",
             "value": value, "unit": "renders/s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1000 * secs / max(1, len(steps)), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "warmup": args.warmup, "ms_per_step": 1000 * cpu["seconds"] / max(1, cpu["steps"]),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": serving_config(args),
-            "cpu_baseline": {"kind": "port", "cores": threads, "value": value, "unit": "renders/s",
-                             "sample": f"per step: requests of the mix in stream order (catalog volumes "
-                                       f"128^3-512^3, 1024^2 captures, new-volume loads with numpy normals) "
-                                       f"for >= {per_step:.1f} s of host work on {threads} threads; "
-                                       f"{reqs} requests ({loads} loads) in {secs:.1f} s",
-                             "samples_per_s": samples / secs if secs else 0.0},
+            "cpu_baseline": {k: cpu[k] for k in ("kind", "cores", "value", "unit", "sample", "samples_per_s")},
             "e2e": {"value": value, "unit": "renders/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
